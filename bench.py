@@ -1,0 +1,355 @@
+"""Benchmark: LMM swaption-portfolio value + all 2*NN Greeks per second on GB300.
+
+Workload (the headline configuration): NN=80 forward rates, NMAT=40 steps,
+delta=0.25, flat L0=0.05, flat lambda=0.2, the 15-swaption portfolio of
+LiborMarketModel/params.h:38-40, 4,194,304 paths per step, FP32 N(0,1) normals
+[paths x 40] resident in HBM (generated once by the library's Philox4x32-10
+generator; synthetic, seeded). A step is one call of the FP32 adjoint:
+forward + payoff adjoint + reverse sweep for every path, value + 80 deltas +
+80 vegas, reduced in FP64.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line (rank 0). `value` is device-resident throughput (normals
+already in HBM, CUDA events on the launching stream); `e2e` is the same metric
+through the host C-ABI call lmm_greeks_f32_host with the normals in pinned host
+memory (host->device copy and result read-back inside the timed region).
+--impl reference times the reference's CPU algorithm for the same workload on
+the host cores (the C restatement under oracle/, since the reference tree is
+not available where this runs).
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import importlib
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "paths/s value+all Greeks: FP32 adjoint vs FP64 bump, 1 GB300, rel err<=1e-4"
+WORKLOAD = 2
+PROFILE_JSON = os.path.join(ROOT, "profiles", "lmm_fused_f32_80x40.json")
+
+# Algorithmic operations per path (reference formulas, liborSwaptionGreeks.cpp),
+# counting a divide and an exp as one operation each, C = cells of the
+# triangle = sum_{n<NMAT} (NN-1-n):
+#   forward  :68-73   9 flops + 1 div + 1 exp   = 11 per cell
+#   deltas   :105-111 10 flops + 2 div          = 12 per cell
+#   vegas    (derived adjoint) 9 flops          =  9 per cell
+#   portfolio_b :120-211                        ~900 per path
+OPS_PER_CELL = 32
+OPS_PORTFOLIO = 900
+
+
+def cells(nn, nmat):
+    return sum(nn - 1 - n for n in range(nmat))
+
+
+def pkg():
+    return importlib.import_module("financial-services-workload-samples_gb300")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r for r in csv.reader(io.StringIO(self.out)) if len(r) >= 9]
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                power.append(float(r[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "power_w_max": max(power) if power else None, "reasons": sorted(reasons)}
+
+
+def cpu_baseline_port(cfg, target_s=3.0, threads=0):
+    """The reference's per-path work (value + delta adjoint) on the host cores,
+    through the oracle's C restatement, on a bounded sample of the workload."""
+    from oracle import oracle as O
+    threads = threads or O.max_threads()
+    calib = 2048
+    z = O.normals_f64(7, calib, cfg.nmat)
+    t0 = time.perf_counter()
+    O.reference_work(cfg, z, calib, threads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    n = int(min(4_194_304, max(calib, calib * target_s / dt)))
+    n = max(16, n - n % 16)
+    z = O.normals_f64(7, n, cfg.nmat)
+    t0 = time.perf_counter()
+    O.reference_work(cfg, z, n, threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "paths/s", "cores": threads, "kind": "port",
+            "sample": f"{n} paths of the same workload (FP64, value + {cfg.nn} deltas by the reference's "
+                      f"adjoint; the reference computes no vegas), {dt:.2f} s wall on {threads} threads",
+            "seconds": dt}
+
+
+def run_reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cfgm = pkg().configs
+    cfg = cfgm.workload(WORKLOAD)
+    from oracle import oracle as O
+    threads = O.max_threads()
+    sample = 65536
+    z = O.normals_f64(11, sample, cfg.nmat)
+    for _ in range(args.warmup):
+        O.reference_work(cfg, z, sample, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.reference_work(cfg, z, sample, threads)
+    dt = time.perf_counter() - t0
+    v = args.steps * sample / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "paths/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: Philox4x32-10 + Box-Muller FP64 normals",
+            "config": {"workload": cfg.name, "nn": cfg.nn, "nmat": cfg.nmat, "paths_per_step": sample,
+                       "work": f"value + {cfg.nn} deltas per path (the reference's adjoint; no vegas)"},
+            "cpu_baseline": {"value": v, "unit": "paths/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} paths per step, FP64, C restatement of "
+                                       "liborSwaptionGreeks.cpp:34-211 with OpenMP over 16-path blocks"},
+            "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    P = pkg()
+    if not os.path.exists(P.LIB_PATH):
+        P.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    cfg = P.configs.workload(WORKLOAD)
+    n, nmat, nout = cfg.paths, cfg.nmat, cfg.nout
+    stream = torch.cuda.current_stream(dev)
+
+    dz = torch.empty(n * nmat, dtype=torch.float32, device=dev)
+    P.normals_f32_device(20260603, n, nmat, dz.data_ptr(), stream=stream.cuda_stream, path0=rank * n)
+    out = torch.zeros(nout, dtype=torch.float64, device=dev)
+    se = torch.zeros(nout, dtype=torch.float64, device=dev)
+    eng = P.Engine(cfg, device=local)
+    eng.set_stream(stream.cuda_stream)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    # ---- device-resident throughput -------------------------------------
+    for _ in range(args.warmup):
+        eng.greeks_f32_device(dz.data_ptr(), n, out.data_ptr(), se.data_ptr())
+    eng.set_timing(True)
+    kern_ms = []
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            eng.greeks_f32_device(dz.data_ptr(), n, out.data_ptr(), se.data_ptr())
+            kern_ms.append(eng.kernel_time()[0]) if args.kernel_times else None
+        ev1.record(stream)
+        barrier()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    launches = args.steps * eng.last_launches
+    # main-kernel duration: time it on separate, event-bracketed calls
+    if not kern_ms:
+        for _ in range(min(args.steps, 20)):
+            eng.greeks_f32_device(dz.data_ptr(), n, out.data_ptr(), se.data_ptr())
+            kern_ms.append(eng.kernel_time()[0])
+    eng.set_timing(False)
+    res32 = out.cpu().numpy().copy()
+    se32 = se.cpu().numpy().copy()
+
+    t_max = elapsed
+    if ws > 1:
+        t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = t.item()
+    value = ws * n * args.steps / t_max
+
+    # ---- end to end through the host C-ABI call, pinned host normals -----
+    hz = torch.empty(n * nmat, dtype=torch.float32, pin_memory=True)
+    hz.copy_(dz)
+    hz_np = hz.numpy()
+    for _ in range(max(1, args.warmup)):
+        eng.greeks_f32(hz_np, n)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.greeks_f32(hz_np, n)
+    e2e_dt = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_dt], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_dt = t.item()
+    e2e = ws * n * args.steps / e2e_dt
+    e2e_launches = eng.last_launches
+
+    # ---- accuracy: FP64 GPU kernel on the identical normals --------------
+    acc = None
+    if rank == 0 and not args.skip_accuracy:
+        dz64 = dz.double()
+        o64 = torch.zeros(nout, dtype=torch.float64, device=dev)
+        eng.greeks_f64_device(dz64.data_ptr(), n, o64.data_ptr())
+        eng.synchronize()
+        r64 = o64.cpu().numpy()
+        del dz64
+        err = []
+        for sl in (slice(0, 1), slice(1, 1 + cfg.nn), slice(1 + cfg.nn, nout)):
+            floor = 1e-2 * np.abs(r64[sl]).max() if r64[sl].size > 1 else 0.0
+            den = np.maximum(np.abs(r64[sl]), floor)
+            den = np.where(den > 0, den, 1.0)
+            err.append(float(np.max(np.abs(res32[sl] - r64[sl]) / den)))
+        acc = {"reference": "FP64 GPU kernel (pinned to the FP64 CPU oracle at 1e-12) on the identical normals",
+               "max_rel_err_value": err[0], "max_rel_err_deltas": err[1], "max_rel_err_vegas": err[2],
+               "tolerance": 1e-4, "rule": "|f32-f64| / max(|f64|, 1% of the largest of its group)",
+               "max_abs_err_over_mc_se": float(np.max(np.abs(res32 - r64) / np.maximum(se32, 1e-300)))}
+
+    # ---- FP64 bump-and-revalue comparator on a bounded sample -------------
+    bump = None
+    if rank == 0 and not args.skip_bump:
+        nb = args.bump_paths
+        dzb = dz[: nb * nmat].double()
+        ob = torch.zeros(nout, dtype=torch.float64, device=dev)
+        eng.bump_greeks_f64_device(dzb.data_ptr(), nb, 1e-6, ob.data_ptr())
+        eng.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        eng.bump_greeks_f64_device(dzb.data_ptr(), nb, 1e-6, ob.data_ptr())
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        bt = s0.elapsed_time(s1) / 1e3
+        bump = {"paths_per_s": nb / bt, "sample_paths": nb, "forward_runs": 1 + 2 * cfg.nn,
+                "seconds": bt, "method": "FP64 forward re-run per bumped input (one-sided, h=1e-6)",
+                "fp32_adjoint_speedup": value / ws / (nb / bt)}
+
+    # ---- roofline -----------------------------------------------------------
+    roof = None
+    if rank == 0:
+        kms = statistics.median(kern_ms)
+        ops = (OPS_PER_CELL * cells(cfg.nn, nmat) + OPS_PORTFOLIO) * n
+        peak = P.fp32_peak_tflops(local, 300.0)
+        traffic = None
+        if os.path.exists(PROFILE_JSON):
+            with open(PROFILE_JSON) as f:
+                prof = json.load(f)
+            traffic = prof.get("dram_bytes_per_launch")
+        achieved = ops / (kms * 1e-3) / 1e12
+        roof = {"bound": "fp32", "kernel": "k_tpp<80,40,hbm,fused>", "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "peak_source": "measured live: FFMA-chain kernel lmm_fp32_peak_tflops (MEASURED_PEAKS.json "
+                               "has no FP32 SIMT figure)",
+                "ops_per_path": OPS_PER_CELL * cells(cfg.nn, nmat) + OPS_PORTFOLIO,
+                "kernel_ms": kms, "algorithmic_bytes_per_launch": 4 * nmat * n,
+                "hbm_gbs_algorithmic": 4 * nmat * n / (kms * 1e-3) / 1e9}
+
+    line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: Philox4x32-10 + Box-Muller N(0,1), FP32 [4194304 x 40] path-major in HBM",
+            "config": {"workload": cfg.name, "nn": cfg.nn, "nmat": nmat, "paths_per_step": n,
+                       "greeks": 2 * cfg.nn, "normals": "HBM, read once per step",
+                       "l2": "inputs larger than L2: 671 MB of normals per step vs 129 MB L2",
+                       "parallelism": f"replicas x{ws} (independent path ranges, no collective)"},
+            "gpu_launches": launches,
+            "e2e": {"value": e2e, "unit": "paths/s", "h2d_bytes_per_step": 4 * n * nmat,
+                    "d2h_bytes_per_step": 2 * 8 * nout + 4, "launches_per_step": e2e_launches,
+                    "api": "lmm_greeks_f32_host (pinned host normals)"},
+            "roofline": roof, "clocks": clk.summary(), "accuracy": acc, "fp64_bump_comparator": bump}
+    if rank == 0 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline_port(cfg, target_s=args.cpu_seconds)
+        line["cpu_baseline"].pop("seconds", None)
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--bump-paths", type=int, default=16384)
+    ap.add_argument("--cpu-seconds", type=float, default=3.0)
+    ap.add_argument("--kernel-times", action="store_true",
+                    help="read the main-kernel time after every timed step (adds a host sync per step)")
+    ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--skip-bump", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,784 @@
+// C-ABI host layer of the GB300 LMM engine (declared in include/lmm_gb300.h).
+//
+// Owns parameter validation, the device-resident model (params.h as data),
+// the engine stream, scratch buffers, the path partition of each launch, and
+// the two entry points with the reference's signature
+// (LiborMarketModel/liborSwaptionGreeks.hpp:12-13). No CPU fallback exists:
+// every compute call runs the CUDA kernels or returns an error.
+#include "lmm_gb300.h"
+#include "lmm_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+using lmm::DevModel;
+using lmm::Mode;
+using lmm::Work;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return LMM_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return LMM_ERR_NO_DEVICE;
+    return LMM_ERR_CUDA;
+}
+
+#define LMM_CK(call)                                         \
+    do {                                                     \
+        cudaError_t lmm_e_ = (call);                         \
+        if (lmm_e_ != cudaSuccess) return cuda_fail(lmm_e_, #call); \
+    } while (0)
+
+#define LMM_TRY(call)                    \
+    do {                                 \
+        int lmm_rc_ = (call);            \
+        if (lmm_rc_ != LMM_OK) return lmm_rc_; \
+    } while (0)
+
+// Growable device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n)
+    {
+        if (n <= bytes) return LMM_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return cuda_fail(e, "cudaMalloc");
+        }
+        bytes = n;
+        return LMM_OK;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T *as() const { return static_cast<T *>(p); }
+};
+
+constexpr int64_t kMaxPaths = int64_t(1) << 40;
+
+}  // namespace
+
+struct lmm_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int nn = 0, nmat = 0, nopt = 0, nscen = 0;
+    double delta = 0.0;
+    int sms = 0;
+    DevModel dm{};
+    DevBuf model;                  // all model arrays
+    DevBuf partial, z32, z64, out, se, flag, vbar;
+    std::map<int, int> bps;        // cached blocks per SM per kernel variant
+    int32_t last_launches = 0;
+    bool timing = false;
+    bool timed = false;            // the last call recorded its events
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // begin, main kernel done, all done
+};
+
+struct lmm_tape {
+    lmm_engine *e = nullptr;
+    int64_t paths = 0;
+    DevBuf buf;
+};
+
+namespace {
+
+int validate(const lmm_params *p)
+{
+    if (!p) return fail(LMM_ERR_INVALID_ARG, "params is NULL");
+    if (p->nn < 2 || p->nn > LMM_MAX_NN)
+        return fail(LMM_ERR_INVALID_ARG, "nn must be in [2, " + std::to_string(LMM_MAX_NN) + "]");
+    if (p->nmat < 1 || p->nmat >= p->nn) return fail(LMM_ERR_INVALID_ARG, "nmat must be in [1, nn-1]");
+    if (p->nopt < 0 || p->nopt > LMM_MAX_NOPT)
+        return fail(LMM_ERR_INVALID_ARG, "nopt must be in [0, " + std::to_string(LMM_MAX_NOPT) + "]");
+    if (p->nscen < 1 || p->nscen > LMM_MAX_SCEN)
+        return fail(LMM_ERR_INVALID_ARG, "nscen must be in [1, " + std::to_string(LMM_MAX_SCEN) + "]");
+    if (!(p->delta > 0.0) || !std::isfinite(p->delta)) return fail(LMM_ERR_INVALID_ARG, "delta must be finite and > 0");
+    if (!p->L0 || !p->lambda) return fail(LMM_ERR_INVALID_ARG, "L0 and lambda are required");
+    if (p->nopt > 0 && (!p->maturities || !p->swaprates))
+        return fail(LMM_ERR_INVALID_ARG, "maturities and swaprates are required when nopt > 0");
+    for (int64_t i = 0; i < (int64_t)p->nscen * p->nn; ++i)
+        if (!(p->L0[i] > 0.0) || !std::isfinite(p->L0[i]))
+            return fail(LMM_ERR_INVALID_ARG, "L0[" + std::to_string(i) + "] must be finite and > 0");
+    for (int i = 0; i < p->nn; ++i)
+        if (!(p->lambda[i] >= 0.0) || !std::isfinite(p->lambda[i]))
+            return fail(LMM_ERR_INVALID_ARG, "lambda[" + std::to_string(i) + "] must be finite and >= 0");
+    for (int o = 0; o < p->nopt; ++o) {
+        if (p->maturities[o] < 1 || p->maturities[o] > p->nn - p->nmat)
+            return fail(LMM_ERR_INVALID_ARG, "maturities[" + std::to_string(o) +
+                                                 "] must be in [1, nn-nmat]: the swap reads rates nmat.."
+                                                 "nmat+m-1 (liborSwaptionGreeks.cpp:133,161)");
+        if (!std::isfinite(p->swaprates[o]))
+            return fail(LMM_ERR_INVALID_ARG, "swaprates[" + std::to_string(o) + "] must be finite");
+    }
+    return LMM_OK;
+}
+
+int set_device(const lmm_engine *e)
+{
+    LMM_CK(cudaSetDevice(e->device));
+    return LMM_OK;
+}
+
+void mark(lmm_engine *e, int i)
+{
+    if (e->timing) cudaEventRecord(e->ev[i], e->stream);
+    if (i == 2) e->timed = e->timing;
+}
+
+// Kernel variant keys for the blocks-per-SM cache.
+int variant_key(int family, Mode mode, bool philox) { return family * 16 + (int)mode * 2 + (philox ? 1 : 0); }
+
+int f32_family(const lmm_engine *e)
+{
+    if (lmm::f32_tpp_supports(e->nn, e->nmat)) return 1;
+    if (lmm::f32_wpp_supports(e->nn, e->nmat)) return 2;
+    return 0;
+}
+
+int blocks_per_sm(lmm_engine *e, int family, Mode mode, bool philox, int *out)
+{
+    const int key = variant_key(family, mode, philox);
+    auto it = e->bps.find(key);
+    if (it != e->bps.end()) {
+        *out = it->second;
+        return LMM_OK;
+    }
+    int b = 0;
+    cudaError_t err;
+    if (family == 1) err = lmm::tpp_blocks_per_sm(mode, philox, &b);
+    else if (family == 2) err = lmm::wpp_blocks_per_sm(e->nn, e->nmat, mode, philox, &b);
+    else if (family == 3) err = lmm::f64_blocks_per_sm(false, &b);
+    else err = lmm::f64_blocks_per_sm(true, &b);
+    if (err != cudaSuccess) return cuda_fail(err, "occupancy query");
+    if (b < 1) return fail(LMM_ERR_UNSUPPORTED, "kernel does not fit on this device");
+    e->bps[key] = b;
+    *out = b;
+    return LMM_OK;
+}
+
+// Splits `paths` per virtual scenario into items so that the grid is about
+// `waves` full waves of the device, and sizes the partial-sum scratch.
+int plan(lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int nout, Work *w,
+         int waves = 2)
+{
+    const int64_t cap = (int64_t)e->sms * bps;
+    const int64_t target = std::max<int64_t>(1, cap * waves);
+    int64_t items = std::max<int64_t>(1, (target + nvs - 1) / nvs);
+    int64_t ppt = std::max<int64_t>(1, (paths + block * items - 1) / (block * items));
+    items = (paths + block * ppt - 1) / (block * ppt);
+    if (ppt > INT32_MAX || items > INT32_MAX || nvs * items > INT32_MAX)
+        return fail(LMM_ERR_TOO_LARGE, "launch too large");
+    w->paths = paths;
+    w->items = (int)items;
+    w->ppt = (int)ppt;
+    w->nout = nout;
+    LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)(nvs * items) * 2 * nout));
+    w->partial = e->partial.as<double>();
+    return LMM_OK;
+}
+
+int check_paths(int64_t paths)
+{
+    if (paths < 1) return fail(LMM_ERR_INVALID_ARG, "paths must be >= 1");
+    if (paths > kMaxPaths) return fail(LMM_ERR_TOO_LARGE, "paths must be <= 2^40");
+    return LMM_OK;
+}
+
+int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t path0, bool philox,
+            int64_t paths, float *tape, const double *d_vbar, double *d_mean, double *d_se)
+{
+    LMM_TRY(check_paths(paths));
+    if (!philox && !d_z) return fail(LMM_ERR_INVALID_ARG, "normals pointer is NULL");
+    if (!d_mean) return fail(LMM_ERR_INVALID_ARG, "output pointer is NULL");
+    if (philox && (path0 < 0 || path0 > kMaxPaths)) return fail(LMM_ERR_INVALID_ARG, "path0 out of range");
+    const int fam = f32_family(e);
+    if (fam == 0)
+        return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for nn=" + std::to_string(e->nn) +
+                                             ", nmat=" + std::to_string(e->nmat));
+    LMM_TRY(set_device(e));
+    int bps = 0;
+    LMM_TRY(blocks_per_sm(e, fam, mode, philox, &bps));
+    const int block = fam == 1 ? lmm::tpp_block_threads() : lmm::wpp_block_threads();
+    const int nout = mode == Mode::Fused ? 1 + 2 * e->nn : (mode == Mode::Forward ? 1 : 2 * e->nn);
+    // thread-per-path blocks take `block` paths per batch; warp-per-path blocks take block/32.
+    const int per_batch = fam == 1 ? block : block / 32;
+    Work w{};
+    LMM_TRY(plan(e, e->nscen, paths, per_batch, bps, nout, &w));
+    LMM_TRY(e->flag.ensure(sizeof(int)));
+    LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
+    mark(e, 0);
+    cudaError_t err = fam == 1
+                          ? lmm::launch_tpp_any(e->dm, mode, d_z, seed, path0, philox, w, tape, d_vbar, e->stream)
+                          : lmm::launch_wpp_any(e->dm, mode, d_z, seed, path0, philox, w, tape, d_vbar, e->stream);
+    if (err != cudaSuccess) return cuda_fail(err, "FP32 LMM kernel launch");
+    mark(e, 1);
+    LMM_CK(lmm::launch_finalize(w.partial, e->nscen, w.items, nout, paths, d_mean, d_se,
+                                e->flag.as<int>(), e->stream));
+    mark(e, 2);
+    e->last_launches = 2;
+    return LMM_OK;
+}
+
+// Copies nscen*nout results (and the non-finite flag) back and waits.
+int fetch(lmm_engine *e, int nout, double *out, double *se)
+{
+    const size_t n = (size_t)e->nscen * nout;
+    int flag = 0;
+    LMM_CK(cudaMemcpyAsync(out, e->out.p, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    if (se) LMM_CK(cudaMemcpyAsync(se, e->se.p, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    LMM_CK(cudaMemcpyAsync(&flag, e->flag.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    LMM_CK(cudaStreamSynchronize(e->stream));
+    if (flag) return fail(LMM_ERR_NONFINITE, "a result is NaN or Inf");
+    return LMM_OK;
+}
+
+int ensure_outputs(lmm_engine *e, int nout)
+{
+    const size_t n = sizeof(double) * (size_t)e->nscen * nout;
+    LMM_TRY(e->out.ensure(n));
+    LMM_TRY(e->se.ensure(n));
+    return LMM_OK;
+}
+
+int run_f64(lmm_engine *e, const double *d_z, int64_t paths, double *d_mean, double *d_se)
+{
+    LMM_TRY(check_paths(paths));
+    if (!d_z || !d_mean) return fail(LMM_ERR_INVALID_ARG, "NULL device pointer");
+    LMM_TRY(set_device(e));
+    int bps = 0;
+    LMM_TRY(blocks_per_sm(e, 3, Mode::Fused, false, &bps));
+    const int nout = 1 + 2 * e->nn;
+    Work w{};
+    LMM_TRY(plan(e, e->nscen, paths, lmm::f64_block_threads(), bps, nout, &w));
+    LMM_TRY(e->flag.ensure(sizeof(int)));
+    LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
+    mark(e, 0);
+    LMM_CK(lmm::launch_f64_greeks(e->dm, d_z, w, e->stream));
+    mark(e, 1);
+    LMM_CK(lmm::launch_finalize(w.partial, e->nscen, w.items, nout, paths, d_mean, d_se,
+                                e->flag.as<int>(), e->stream));
+    mark(e, 2);
+    e->last_launches = 2;
+    return LMM_OK;
+}
+
+int run_bump(lmm_engine *e, const double *d_z, int64_t paths, double h, double *d_mean,
+             double *d_se)
+{
+    LMM_TRY(check_paths(paths));
+    if (!d_z || !d_mean) return fail(LMM_ERR_INVALID_ARG, "NULL device pointer");
+    if (!(h > 0.0) || !std::isfinite(h)) return fail(LMM_ERR_INVALID_ARG, "bump h must be finite and > 0");
+    LMM_TRY(set_device(e));
+    int bps = 0;
+    LMM_TRY(blocks_per_sm(e, 4, Mode::Fused, false, &bps));
+    const int nb = 1 + 2 * e->nn;
+    Work w{};
+    LMM_TRY(plan(e, (int64_t)e->nscen * nb, paths, lmm::f64_block_threads(), bps, 1, &w));
+    LMM_TRY(e->flag.ensure(sizeof(int)));
+    LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
+    mark(e, 0);
+    LMM_CK(lmm::launch_f64_bump(e->dm, d_z, h, w, e->stream));
+    mark(e, 1);
+    LMM_CK(lmm::launch_finalize(w.partial, e->nscen * nb, w.items, 1, paths, d_mean, d_se,
+                                e->flag.as<int>(), e->stream));
+    LMM_CK(lmm::launch_bump_diff(d_mean, d_se, e->nscen, nb, h, e->stream));
+    mark(e, 2);
+    e->last_launches = 3;
+    return LMM_OK;
+}
+
+// Process-wide engine with the reference's own parameter set, for the
+// reference-signature entry points.
+std::mutex g_ref_mu;
+lmm_engine *g_ref_engine = nullptr;
+
+const int kRefMat[15] = {4, 4, 4, 8, 8, 8, 20, 20, 20, 28, 28, 28, 40, 40, 40};  // params.h:38
+
+int ref_engine(lmm_engine **out)
+{
+    if (g_ref_engine) {
+        *out = g_ref_engine;
+        return LMM_OK;
+    }
+    // params.h:39-40 spells the strikes as float literals; the FP64 build
+    // therefore prices with their float-rounded values.
+    const float kRateF[3] = {0.045f, 0.05f, 0.055f};
+    double rates[15];
+    for (int o = 0; o < 15; ++o) rates[o] = (double)kRateF[o % 3];
+    std::vector<double> L0(80, 0.051), lam(80, 0.2);  // liborSwaptionGreeks.cpp:270-271
+    lmm_params p{80, 40, 15, 1, 0.25, L0.data(), lam.data(), kRefMat, rates};
+    LMM_TRY(lmm_engine_create(&p, 0, &g_ref_engine));
+    *out = g_ref_engine;
+    return LMM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lmm_validate_params(const lmm_params *p) { return validate(p); }
+
+int64_t lmm_num_outputs(const lmm_params *p) { return p ? 1 + 2 * (int64_t)p->nn : 0; }
+
+const char *lmm_status_string(int s)
+{
+    switch (s) {
+        case LMM_OK: return "ok";
+        case LMM_ERR_INVALID_ARG: return "invalid argument";
+        case LMM_ERR_UNSUPPORTED: return "unsupported";
+        case LMM_ERR_CUDA: return "CUDA error";
+        case LMM_ERR_NONFINITE: return "non-finite result";
+        case LMM_ERR_NO_DEVICE: return "no CUDA device";
+        case LMM_ERR_TOO_LARGE: return "too large";
+        case LMM_ERR_OUT_OF_MEMORY: return "out of device memory";
+        default: return "unknown status";
+    }
+}
+
+const char *lmm_last_error(void) { return g_last_error.c_str(); }
+
+const char *lmm_version(void) { return "0.1.0"; }
+
+int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
+{
+    if (!out) return fail(LMM_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    LMM_TRY(validate(p));
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev == 0) return fail(LMM_ERR_NO_DEVICE, "no CUDA device available");
+    if (device < 0 || device >= ndev) return fail(LMM_ERR_INVALID_ARG, "device index out of range");
+    std::unique_ptr<lmm_engine> e(new lmm_engine());
+    e->device = device;
+    e->nn = p->nn;
+    e->nmat = p->nmat;
+    e->nopt = p->nopt;
+    e->nscen = p->nscen;
+    e->delta = p->delta;
+    LMM_CK(cudaSetDevice(device));
+    LMM_CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, device));
+
+    const int nn = p->nn, nmat = p->nmat, nopt = p->nopt, ns = p->nscen, M = nn - nmat;
+    const double d = p->delta;
+    const double log2e = 1.4426950408889634073599246810019;
+    std::vector<float4> kc(nn);
+    std::vector<float> kd(nn), L0f((size_t)ns * nn), iL0f((size_t)ns * nn);
+    for (int k = 0; k < nn; ++k) {
+        const double l = p->lambda[k];
+        kc[k] = make_float4((float)(l * log2e), (float)(-0.5 * d * l * l * log2e), (float)(d * d * l), (float)l);
+        kd[k] = (float)(d * l);
+    }
+    for (size_t i = 0; i < (size_t)ns * nn; ++i) {
+        L0f[i] = (float)p->L0[i];
+        iL0f[i] = 1.0f / L0f[i];
+    }
+    // options grouped by swap length (CSR over m = maturity-1), stable order
+    std::vector<int> order(nopt);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return p->maturities[a] < p->maturities[b]; });
+    std::vector<int> ost(M + 1, 0);
+    std::vector<float> okf(nopt);
+    std::vector<double> okd(nopt);
+    for (int o = 0; o < nopt; ++o) {
+        ost[p->maturities[order[o]]] += 1;  // count at m+1 = maturity
+        okf[o] = (float)p->swaprates[order[o]];
+        okd[o] = p->swaprates[order[o]];
+    }
+    for (int m = 0; m < M; ++m) ost[m + 1] += ost[m];
+
+    // one allocation, 256-byte aligned sections
+    size_t off = 0;
+    auto sect = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~size_t(255);
+        return o;
+    };
+    const size_t o_kc = sect(sizeof(float4) * nn), o_kd = sect(sizeof(float) * nn);
+    const size_t o_l0f = sect(sizeof(float) * L0f.size()), o_il0f = sect(sizeof(float) * iL0f.size());
+    const size_t o_l0d = sect(sizeof(double) * L0f.size()), o_lamd = sect(sizeof(double) * nn);
+    const size_t o_ost = sect(sizeof(int) * (M + 1)), o_okf = sect(sizeof(float) * std::max(1, nopt));
+    const size_t o_okd = sect(sizeof(double) * std::max(1, nopt));
+    LMM_TRY(e->model.ensure(off));
+    char *base = e->model.as<char>();
+    auto up = [&](size_t o, const void *src, size_t bytes) {
+        return bytes ? cudaMemcpy(base + o, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+    };
+    LMM_CK(up(o_kc, kc.data(), sizeof(float4) * nn));
+    LMM_CK(up(o_kd, kd.data(), sizeof(float) * nn));
+    LMM_CK(up(o_l0f, L0f.data(), sizeof(float) * L0f.size()));
+    LMM_CK(up(o_il0f, iL0f.data(), sizeof(float) * iL0f.size()));
+    LMM_CK(up(o_l0d, p->L0, sizeof(double) * L0f.size()));
+    LMM_CK(up(o_lamd, p->lambda, sizeof(double) * nn));
+    LMM_CK(up(o_ost, ost.data(), sizeof(int) * (M + 1)));
+    LMM_CK(up(o_okf, okf.data(), sizeof(float) * nopt));
+    LMM_CK(up(o_okd, okd.data(), sizeof(double) * nopt));
+
+    DevModel &m = e->dm;
+    m.nn = nn;
+    m.nmat = nmat;
+    m.nopt = nopt;
+    m.nscen = ns;
+    m.delta = (float)d;
+    m.sqd = (float)std::sqrt(d);
+    m.d2 = (float)(d * d);
+    m.deltad = d;
+    m.sqdd = std::sqrt(d);
+    m.kc = reinterpret_cast<const float4 *>(base + o_kc);
+    m.kd = reinterpret_cast<const float *>(base + o_kd);
+    m.L0f = reinterpret_cast<const float *>(base + o_l0f);
+    m.invL0f = reinterpret_cast<const float *>(base + o_il0f);
+    m.L0d = reinterpret_cast<const double *>(base + o_l0d);
+    m.lamd = reinterpret_cast<const double *>(base + o_lamd);
+    m.opt_start = reinterpret_cast<const int *>(base + o_ost);
+    m.optKf = reinterpret_cast<const float *>(base + o_okf);
+    m.optKd = reinterpret_cast<const double *>(base + o_okd);
+
+    LMM_CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    e->own_stream = true;
+    *out = e.release();
+    return LMM_OK;
+}
+
+int lmm_engine_destroy(lmm_engine *e)
+{
+    if (!e) return LMM_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    e->model.release();
+    e->partial.release();
+    e->z32.release();
+    e->z64.release();
+    e->out.release();
+    e->se.release();
+    e->flag.release();
+    e->vbar.release();
+    if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+    for (auto &ev : e->ev)
+        if (ev) cudaEventDestroy(ev);
+    delete e;
+    return LMM_OK;
+}
+
+int lmm_engine_set_stream(lmm_engine *e, void *stream)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    LMM_TRY(set_device(e));
+    if (e->own_stream && e->stream) {
+        LMM_CK(cudaStreamSynchronize(e->stream));
+        LMM_CK(cudaStreamDestroy(e->stream));
+    }
+    e->stream = static_cast<cudaStream_t>(stream);
+    e->own_stream = false;
+    return LMM_OK;
+}
+
+int lmm_engine_synchronize(lmm_engine *e)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    LMM_TRY(set_device(e));
+    LMM_CK(cudaStreamSynchronize(e->stream));
+    return LMM_OK;
+}
+
+int32_t lmm_engine_last_launches(const lmm_engine *e) { return e ? e->last_launches : 0; }
+
+int lmm_engine_set_timing(lmm_engine *e, int32_t enable)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    LMM_TRY(set_device(e));
+    if (enable && !e->ev[0])
+        for (auto &ev : e->ev) LMM_CK(cudaEventCreate(&ev));
+    e->timing = enable != 0;
+    e->timed = false;
+    return LMM_OK;
+}
+
+int lmm_engine_kernel_time(lmm_engine *e, double *main_kernel_ms, double *total_ms)
+{
+    if (!e || !main_kernel_ms) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
+    if (!e->timed) return fail(LMM_ERR_INVALID_ARG, "no timed call: enable timing first");
+    LMM_TRY(set_device(e));
+    LMM_CK(cudaEventSynchronize(e->ev[2]));
+    float a = 0.0f, b = 0.0f;
+    LMM_CK(cudaEventElapsedTime(&a, e->ev[0], e->ev[1]));
+    LMM_CK(cudaEventElapsedTime(&b, e->ev[0], e->ev[2]));
+    *main_kernel_ms = a;
+    if (total_ms) *total_ms = b;
+    return LMM_OK;
+}
+
+int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops)
+{
+    if (!tflops || !(ms > 0.0)) return fail(LMM_ERR_INVALID_ARG, "need tflops and ms > 0");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(LMM_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= ndev) return fail(LMM_ERR_INVALID_ARG, "device index out of range");
+    LMM_CK(cudaSetDevice(device));
+    int sms = 0;
+    LMM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const int blocks = sms * 8;                  // 8 x 256 threads per SM
+    DevBuf sink;
+    LMM_TRY(sink.ensure(sizeof(float) * (size_t)blocks * 256));
+    cudaStream_t st;
+    LMM_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    auto run = [&](int iters, float *out_ms) -> cudaError_t {
+        cudaEventRecord(a, st);
+        cudaError_t err = lmm::launch_ffma_peak(blocks, iters, 0.9999f, 1e-4f, sink.as<float>(), st);
+        cudaEventRecord(b, st);
+        if (err != cudaSuccess) return err;
+        err = cudaEventSynchronize(b);
+        if (err != cudaSuccess) return err;
+        return cudaEventElapsedTime(out_ms, a, b);
+    };
+    float t = 0.0f;
+    int iters = 4096;
+    cudaError_t err = run(iters, &t);           // warm-up and calibration
+    if (err == cudaSuccess && t > 0.0f) {
+        iters = (int)std::min(1e8, std::max(4096.0, iters * ms / t));
+        err = run(iters, &t);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaStreamDestroy(st);
+    sink.release();
+    if (err != cudaSuccess) return cuda_fail(err, "FFMA peak probe");
+    const double flops = 2.0 * 16.0 * (double)iters * blocks * 256.0;
+    *tflops = flops / (t * 1e-3) / 1e12;
+    return LMM_OK;
+}
+
+// ---- FP32 adjoint ----------------------------------------------------------
+
+int lmm_greeks_f32_device(lmm_engine *e, const float *d_z, int64_t paths, double *d_out, double *d_se)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    return run_f32(e, Mode::Fused, d_z, 0, 0, false, paths, nullptr, nullptr, d_out, d_se);
+}
+
+int lmm_greeks_f32_host(lmm_engine *e, const float *z, int64_t paths, double *out, double *se)
+{
+    if (!e || !z || !out) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
+    LMM_TRY(check_paths(paths));
+    LMM_TRY(set_device(e));
+    const size_t zb = sizeof(float) * (size_t)paths * e->nmat;
+    LMM_TRY(e->z32.ensure(zb));
+    LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
+    LMM_CK(cudaMemcpyAsync(e->z32.p, z, zb, cudaMemcpyHostToDevice, e->stream));
+    LMM_TRY(run_f32(e, Mode::Fused, e->z32.as<float>(), 0, 0, false, paths, nullptr, nullptr,
+                    e->out.as<double>(), e->se.as<double>()));
+    return fetch(e, 1 + 2 * e->nn, out, se);
+}
+
+int lmm_greeks_philox_device(lmm_engine *e, uint64_t seed, int64_t path0, int64_t paths,
+                             double *d_out, double *d_se)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    return run_f32(e, Mode::Fused, nullptr, seed, path0, true, paths, nullptr, nullptr, d_out, d_se);
+}
+
+int lmm_greeks_philox_host(lmm_engine *e, uint64_t seed, int64_t path0, int64_t paths, double *out,
+                           double *se)
+{
+    if (!e || !out) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
+    LMM_TRY(check_paths(paths));
+    LMM_TRY(set_device(e));
+    LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
+    LMM_TRY(run_f32(e, Mode::Fused, nullptr, seed, path0, true, paths, nullptr, nullptr,
+                    e->out.as<double>(), e->se.as<double>()));
+    return fetch(e, 1 + 2 * e->nn, out, se);
+}
+
+// ---- forward/backward pair ---------------------------------------------------
+
+int lmm_tape_create(lmm_engine *e, int64_t paths, lmm_tape **out)
+{
+    if (!e || !out) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    LMM_TRY(check_paths(paths));
+    LMM_TRY(set_device(e));
+    std::unique_ptr<lmm_tape> t(new lmm_tape());
+    t->e = e;
+    t->paths = paths;
+    LMM_TRY(t->buf.ensure(sizeof(float) * (size_t)(e->nn + e->nmat) * e->nscen * (size_t)paths));
+    *out = t.release();
+    return LMM_OK;
+}
+
+int lmm_tape_destroy(lmm_tape *t)
+{
+    if (!t) return LMM_OK;
+    cudaSetDevice(t->e->device);
+    t->buf.release();
+    delete t;
+    return LMM_OK;
+}
+
+int lmm_forward_f32_device(lmm_engine *e, const float *d_z, int64_t paths, lmm_tape *t,
+                           double *d_value, double *d_value_se)
+{
+    if (!e || !t) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
+    if (t->e != e || t->paths != paths) return fail(LMM_ERR_INVALID_ARG, "tape belongs to another engine or size");
+    return run_f32(e, Mode::Forward, d_z, 0, 0, false, paths, t->buf.as<float>(), nullptr, d_value,
+                   d_value_se);
+}
+
+int lmm_backward_f32_device(lmm_engine *e, const float *d_z, const lmm_tape *t,
+                            const double *value_bar, double *d_grad, double *d_grad_se)
+{
+    if (!e || !t || !value_bar) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
+    if (t->e != e) return fail(LMM_ERR_INVALID_ARG, "tape belongs to another engine");
+    for (int s = 0; s < e->nscen; ++s)
+        if (!std::isfinite(value_bar[s])) return fail(LMM_ERR_INVALID_ARG, "value_bar must be finite");
+    LMM_TRY(set_device(e));
+    LMM_TRY(e->vbar.ensure(sizeof(double) * e->nscen));
+    LMM_CK(cudaMemcpyAsync(e->vbar.p, value_bar, sizeof(double) * e->nscen, cudaMemcpyHostToDevice,
+                           e->stream));
+    return run_f32(e, Mode::Backward, d_z, 0, 0, false, t->paths, const_cast<float *>(t->buf.as<float>()),
+                   e->vbar.as<double>(), d_grad, d_grad_se);
+}
+
+// ---- FP64 -------------------------------------------------------------------
+
+int lmm_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, double *d_out, double *d_se)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    return run_f64(e, d_z, paths, d_out, d_se);
+}
+
+int lmm_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double *out, double *se)
+{
+    if (!e || !z || !out) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
+    LMM_TRY(check_paths(paths));
+    LMM_TRY(set_device(e));
+    const size_t zb = sizeof(double) * (size_t)paths * e->nmat;
+    LMM_TRY(e->z64.ensure(zb));
+    LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
+    LMM_CK(cudaMemcpyAsync(e->z64.p, z, zb, cudaMemcpyHostToDevice, e->stream));
+    LMM_TRY(run_f64(e, e->z64.as<double>(), paths, e->out.as<double>(), e->se.as<double>()));
+    return fetch(e, 1 + 2 * e->nn, out, se);
+}
+
+int lmm_bump_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, double h,
+                               double *d_out, double *d_se)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    return run_bump(e, d_z, paths, h, d_out, d_se);
+}
+
+int lmm_bump_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double h, double *out,
+                             double *se)
+{
+    if (!e || !z || !out) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
+    LMM_TRY(check_paths(paths));
+    LMM_TRY(set_device(e));
+    const size_t zb = sizeof(double) * (size_t)paths * e->nmat;
+    LMM_TRY(e->z64.ensure(zb));
+    LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
+    LMM_CK(cudaMemcpyAsync(e->z64.p, z, zb, cudaMemcpyHostToDevice, e->stream));
+    LMM_TRY(run_bump(e, e->z64.as<double>(), paths, h, e->out.as<double>(), e->se.as<double>()));
+    return fetch(e, 1 + 2 * e->nn, out, se);
+}
+
+// ---- normals -------------------------------------------------------------------
+
+int lmm_normals_f32_device(uint64_t seed, int64_t path0, int64_t paths, int32_t nmat, float *d_z,
+                           void *stream)
+{
+    if (!d_z || paths < 1 || nmat < 1 || path0 < 0) return fail(LMM_ERR_INVALID_ARG, "bad normals request");
+    LMM_CK(lmm::launch_normals_f32(seed, path0, paths, nmat, 0.0f, 1.0f, d_z,
+                                   static_cast<cudaStream_t>(stream)));
+    return LMM_OK;
+}
+
+int lmm_normals_f64_device(uint64_t seed, int64_t path0, int64_t paths, int32_t nmat, double mean,
+                           double std_dev, double *d_z, void *stream)
+{
+    if (!d_z || paths < 1 || nmat < 1 || path0 < 0 || !std::isfinite(mean) || !std::isfinite(std_dev))
+        return fail(LMM_ERR_INVALID_ARG, "bad normals request");
+    LMM_CK(lmm::launch_normals_f64(seed, path0, paths, nmat, mean, std_dev, d_z,
+                                   static_cast<cudaStream_t>(stream)));
+    return LMM_OK;
+}
+
+// ---- the reference's signature ----------------------------------------------------
+
+int lmm_swaption_greeks(double *z, int num, double mean, double std_dev, int seed, double *d_v,
+                        double *d_Lb, int numPaths)
+{
+    (void)seed;  // ignored, as in the reference (generateRand uses its default key)
+    if (!z || !d_v || !d_Lb || numPaths < 1 || (int64_t)num != 40 * (int64_t)numPaths)
+        return fail(LMM_ERR_INVALID_ARG, "need z[40*numPaths], d_v, d_Lb and numPaths >= 1");
+    std::lock_guard<std::mutex> lk(g_ref_mu);
+    lmm_engine *e = nullptr;
+    LMM_TRY(ref_engine(&e));
+    LMM_TRY(set_device(e));
+    LMM_TRY(e->z64.ensure(sizeof(double) * (size_t)num));
+    LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
+    LMM_CK(lmm::launch_normals_f64(12345u, 0, numPaths, 40, mean, std_dev, e->z64.as<double>(), e->stream));
+    LMM_CK(cudaMemcpyAsync(z, e->z64.p, sizeof(double) * (size_t)num, cudaMemcpyDeviceToHost, e->stream));
+    LMM_TRY(run_f64(e, e->z64.as<double>(), numPaths, e->out.as<double>(), e->se.as<double>()));
+    std::vector<double> out(1 + 2 * e->nn);
+    LMM_TRY(fetch(e, 1 + 2 * e->nn, out.data(), nullptr));
+    *d_v = out[0];
+    *d_Lb = out[e->nn];
+    return LMM_OK;
+}
+
+int lmm_swaption_greeks_f32(float *z, int num, float mean, float std_dev, int seed, float *d_v,
+                            float *d_Lb, int numPaths)
+{
+    (void)seed;
+    if (!z || !d_v || !d_Lb || numPaths < 1 || (int64_t)num != 40 * (int64_t)numPaths)
+        return fail(LMM_ERR_INVALID_ARG, "need z[40*numPaths], d_v, d_Lb and numPaths >= 1");
+    if (!std::isfinite(mean) || !std::isfinite(std_dev)) return fail(LMM_ERR_INVALID_ARG, "mean/std_dev must be finite");
+    std::lock_guard<std::mutex> lk(g_ref_mu);
+    lmm_engine *e = nullptr;
+    LMM_TRY(ref_engine(&e));
+    LMM_TRY(set_device(e));
+    LMM_TRY(e->z32.ensure(sizeof(float) * (size_t)num));
+    LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
+    LMM_CK(lmm::launch_normals_f32(12345u, 0, numPaths, 40, mean, std_dev, e->z32.as<float>(), e->stream));
+    LMM_CK(cudaMemcpyAsync(z, e->z32.p, sizeof(float) * (size_t)num, cudaMemcpyDeviceToHost, e->stream));
+    LMM_TRY(run_f32(e, Mode::Fused, e->z32.as<float>(), 0, 0, false, numPaths, nullptr, nullptr,
+                    e->out.as<double>(), e->se.as<double>()));
+    std::vector<double> out(1 + 2 * e->nn);
+    LMM_TRY(fetch(e, 1 + 2 * e->nn, out.data(), nullptr));
+    *d_v = (float)out[0];
+    *d_Lb = (float)out[e->nn];
+    return LMM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,104 @@
+// Device helpers shared by the LMM kernels: PTX fast math, Philox4x32-10,
+// Box-Muller, warp reductions.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lmm_internal.h"
+
+namespace lmm {
+
+// MUFU approximations issued directly (PTX ISA: rcp.approx.ftz.f32,
+// ex2.approx.ftz.f32). Both are within a few ulp in FP32.
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): multipliers 0xD2511F53,
+// 0xCD9E8D57 and Weyl key increments 0x9E3779B9, 0xBB67AE85, ten rounds.
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    }
+    return c;
+}
+
+// The counter layout of the library: normals 4q..4q+3 of global path p.
+__device__ __forceinline__ U4 philox_quad(uint64_t seed, uint64_t path, uint32_t q)
+{
+    return philox4x32_10(U4{q, 0u, (uint32_t)path, (uint32_t)(path >> 32)}, (uint32_t)seed,
+                         (uint32_t)(seed >> 32));
+}
+
+// FP32 Box-Muller on 24-bit uniforms: u1 = ((a>>8)+1)/2^24 in (0,1],
+// u2 = (b>>8)/2^24 in [0,1); z0 = r cos(2 pi u2), z1 = r sin(2 pi u2).
+__device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float &z0, float &z1)
+{
+    const float u1 = (float)((a >> 8) + 1u) * 5.9604644775390625e-8f;
+    const float u2 = (float)(b >> 8) * 5.9604644775390625e-8f;
+    const float r = sqrtf(-2.0f * logf(u1));
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    z0 = r * c;
+    z1 = r * s;
+}
+
+__device__ __forceinline__ void normals_quad_f32(uint64_t seed, uint64_t path, uint32_t q,
+                                                 float z[4])
+{
+    const U4 x = philox_quad(seed, path, q);
+    box_muller_f32(x.x, x.y, z[0], z[1]);
+    box_muller_f32(x.z, x.w, z[2], z[3]);
+}
+
+// FP64 Box-Muller on 32-bit uniforms (the FP64 spec of the library).
+__device__ __forceinline__ void box_muller_f64(uint32_t a, uint32_t b, double &z0, double &z1)
+{
+    const double u1 = ((double)a + 1.0) * 2.3283064365386962890625e-10;
+    const double u2 = (double)b * 2.3283064365386962890625e-10;
+    const double r = sqrt(-2.0 * log(u1));
+    const double th = 6.283185307179586476925286766559 * u2;
+    double s, c;
+    sincos(th, &s, &c);
+    z0 = r * c;
+    z1 = r * s;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace lmm

@@ -1,0 +1,91 @@
+// Internal interface between the C-ABI host layer (lmm_capi.cpp) and the
+// CUDA translation units. Plain C++ types only; no device code.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lmm {
+
+constexpr int kMaxNN = 256;
+constexpr int kMaxNopt = 64;
+
+// Per-engine model data resident in HBM, passed to kernels by value.
+// Per time-to-maturity k (the reference's lambda[i-n-1] index):
+//   kc[k] = { lambda_k*log2(e), -delta*lambda_k^2*log2(e)/2, delta^2*lambda_k, lambda_k }
+//   kd[k] = delta*lambda_k
+// so that one Euler cell (liborSwaptionGreeks.cpp:68-73) is
+//   t = L/(1+delta L); V += kc.z*t; L *= 2^(kc.x*(V + sqrt(delta) z) + kc.y)
+// with V = delta * (the reference's running sum v).
+struct DevModel {
+    int nn, nmat, nopt, nscen;
+    float delta, sqd, d2;                 // delta, sqrt(delta), delta^2
+    double deltad, sqdd;
+    const float4 *kc;                     // [nn]
+    const float *kd;                      // [nn]
+    const float *L0f;                     // [nscen][nn]
+    const float *invL0f;                  // [nscen][nn]
+    const double *L0d;                    // [nscen][nn]
+    const double *lamd;                   // [nn]
+    const int *opt_start;                 // [nn-nmat+1] options grouped by maturity-1 (CSR)
+    const float *optKf;                   // [nopt] strikes in that grouped order
+    const double *optKd;                  // [nopt]
+};
+
+// Path partition of one launch: grid = nscen * items blocks; block b takes
+// scenario b / items and the path range [item*ipaths, (item+1)*ipaths) of it.
+struct Work {
+    int64_t paths;        // per scenario
+    int items;            // items per scenario
+    int ppt;              // paths per thread per item
+    double *partial;      // [nscen*items][2*nout]: per-item sums and sums of squares
+    int nout;             // outputs per scenario reduced by this launch
+};
+
+enum class Mode : int { Fused = 0, Forward = 1, Backward = 2 };
+
+// FP32 thread-per-path kernels (lmm_f32_tpp.cu, NN=80, NMAT=40).
+bool f32_tpp_supports(int nn, int nmat);
+int tpp_block_threads();
+cudaError_t tpp_blocks_per_sm(Mode mode, bool philox, int *blocks);
+cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
+                           int64_t path0, bool philox, const Work &w, float *tape,
+                           const double *vbar, cudaStream_t s);
+// FP32 warp-per-path kernels (lmm_f32_wpp.cu, any NN <= kMaxNN, reverse sweep
+// recomputed from checkpoints every kWppCkpt steps).
+bool f32_wpp_supports(int nn, int nmat);
+int wpp_block_threads();
+cudaError_t wpp_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks);
+cudaError_t launch_wpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
+                           int64_t path0, bool philox, const Work &w, float *tape,
+                           const double *vbar, cudaStream_t s);
+
+// FP64 kernels: thread per path, runtime shape.
+int f64_block_threads();
+cudaError_t f64_blocks_per_sm(bool bump, int *blocks);
+cudaError_t launch_f64_greeks(const DevModel &m, const double *z, const Work &w, cudaStream_t s);
+// Bumped forward re-runs: 1 + 2nn variants per scenario; the launch's
+// virtual scenarios are (scenario, variant) and each reduces one output, the
+// variant's value (w.nout = 1).
+cudaError_t launch_f64_bump(const DevModel &m, const double *z, double h, const Work &w,
+                            cudaStream_t s);
+
+// Sums the per-item partials of each scenario in a fixed order and writes
+// mean and standard error; sets *flag if a result is not finite.
+cudaError_t launch_finalize(const double *partial, int nscen, int items, int nout, int64_t paths,
+                            double *mean, double *se, int *flag, cudaStream_t s);
+// Turns bumped means into one-sided differences in place: out[j] =
+// (out[j]-out[0])/h for j >= 1, per scenario.
+cudaError_t launch_bump_diff(double *mean, double *se, int nscen, int nout, double h,
+                             cudaStream_t s);
+
+// FFMA throughput probe: `blocks` x 256 threads, `iters` iterations of 16
+// independent FMA chains each; one float per thread to `sink`.
+cudaError_t launch_ffma_peak(int blocks, int iters, float a, float b, float *sink, cudaStream_t s);
+
+cudaError_t launch_normals_f32(uint64_t seed, int64_t path0, int64_t paths, int nmat, float mean,
+                               float sd, float *z, cudaStream_t s);
+cudaError_t launch_normals_f64(uint64_t seed, int64_t path0, int64_t paths, int nmat, double mean,
+                               double sd, double *z, cudaStream_t s);
+
+}  // namespace lmm

@@ -1,0 +1,189 @@
+/*
+ * lmm_gb300.h -- C ABI of the GB300 (sm_103a) LIBOR Market Model
+ * swaption-portfolio Monte Carlo with pathwise adjoint Greeks.
+ *
+ * Drop-in boundary for intel/Financial-Services-Workload-Samples,
+ * LiborMarketModel: the reference exposes exactly one entry point,
+ *
+ *   void liborSwaptionGreeks(REAL *z, int num, REAL mean, REAL std_dev,
+ *                            int seed, REAL *d_v, REAL *d_Lb, int numPaths);
+ *   (LiborMarketModel/liborSwaptionGreeks.hpp:12-13, defined at
+ *    liborSwaptionGreeks.cpp:241-368)
+ *
+ * whose compute is path_calc_b1 (:34-82), portfolio_b (:120-211) and
+ * path_calc_b2 (:86-117), with the model fixed at compile time by
+ * LiborMarketModel/params.h:10-40 and the curve hard-coded at :269-271.
+ * lmm_swaption_greeks / lmm_swaption_greeks_f32 below keep that signature.
+ * The engine API generalises it: runtime model/portfolio (params.h as a
+ * struct), all NN deltas AND all NN vegas (the reference returns one delta
+ * and no vega), scenario batches, device-resident inputs, and a
+ * forward/backward pair.
+ *
+ * Conventions
+ *   - Every call returns an int status (LMM_OK = 0, negative on error); no
+ *     exception or abort crosses the ABI. lmm_last_error() gives detail.
+ *   - Results: for each scenario s, out[s*(1+2nn) + j] with j = 0 the
+ *     discounted portfolio value, j = 1+i the delta dV/dL0[i], j = 1+nn+k
+ *     the vega dV/dlambda[k] (lambda indexed by time to maturity, as the
+ *     reference reads lambda[i-n-1], liborSwaptionGreeks.cpp:65,102).
+ *     Values are Monte Carlo means over the paths; se (may be NULL) holds
+ *     their standard errors in the same layout.
+ *   - Normals are path-major, z[p*nmat + n], as in the reference
+ *     (liborSwaptionGreeks.cpp:56). All scenarios of an engine use the same
+ *     normals (common random numbers).
+ *   - *_host calls take host pointers and block until results are back.
+ *     *_device calls take device pointers, are enqueued on the engine's
+ *     stream and return without waiting.
+ *   - One engine is not thread-safe; distinct engines are independent.
+ */
+#ifndef LMM_GB300_H
+#define LMM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    LMM_OK = 0,
+    LMM_ERR_INVALID_ARG = -1,   /* bad pointer, size or parameter value       */
+    LMM_ERR_UNSUPPORTED = -2,   /* shape or option the kernels do not cover   */
+    LMM_ERR_CUDA = -3,          /* a CUDA runtime call failed                 */
+    LMM_ERR_NONFINITE = -4,     /* a result came out NaN or Inf               */
+    LMM_ERR_NO_DEVICE = -5,     /* no usable CUDA device                      */
+    LMM_ERR_TOO_LARGE = -6,     /* size beyond a documented limit             */
+    LMM_ERR_OUT_OF_MEMORY = -7  /* device allocation failed                   */
+};
+
+/* Limits. */
+#define LMM_MAX_NN 256          /* forward rates                               */
+#define LMM_MAX_NOPT 64         /* swaptions per portfolio                     */
+#define LMM_MAX_SCEN 65536      /* initial curves per engine                   */
+
+/* The model and portfolio: LiborMarketModel/params.h:27-40 as runtime data,
+ * plus the curve and vols that liborSwaptionGreeks.cpp:269-271 hard-codes. */
+typedef struct lmm_params {
+    int32_t nn;                 /* NN, number of forward rates (params.h:27)      */
+    int32_t nmat;               /* NMAT, time steps = normals per path (:28)      */
+    int32_t nopt;               /* NOPT, swaptions (:30)                          */
+    int32_t nscen;              /* initial curves; 1 for a single valuation       */
+    double delta;               /* DELTA, accrual fraction (:33); sqrt(delta)
+                                   replaces SQRT_DELTA (:34)                      */
+    const double *L0;           /* [nscen][nn] initial forward curves (:271)      */
+    const double *lambda;       /* [nn] vol by time to maturity (:270)            */
+    const int32_t *maturities;  /* [nopt] swap length in periods, 1..nn-nmat (:38) */
+    const double *swaprates;    /* [nopt] strikes (:39-40)                        */
+} lmm_params;
+
+typedef struct lmm_engine lmm_engine;
+typedef struct lmm_tape lmm_tape;
+
+/* ---- housekeeping ---------------------------------------------------- */
+
+/* Checks a parameter set on the host only (no GPU needed). */
+int lmm_validate_params(const lmm_params *p);
+/* Number of doubles per scenario in a result: 1 + 2*nn. */
+int64_t lmm_num_outputs(const lmm_params *p);
+const char *lmm_status_string(int status);
+/* Detail of the last failure on the calling thread ("" if none). */
+const char *lmm_last_error(void);
+/* Library version as "major.minor.patch". */
+const char *lmm_version(void);
+
+/* Uploads the parameters to `device` and creates the engine's own stream. */
+int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out);
+int lmm_engine_destroy(lmm_engine *e);
+/* Use `stream` (a cudaStream_t, NULL = legacy default stream) from now on. */
+int lmm_engine_set_stream(lmm_engine *e, void *stream);
+/* Blocks until all work enqueued on the engine's stream is done. */
+int lmm_engine_synchronize(lmm_engine *e);
+/* Launches enqueued by the last compute call (kernels only). */
+int32_t lmm_engine_last_launches(const lmm_engine *e);
+/* Tracing: with timing on, every compute call brackets its main kernel and
+ * its whole launch sequence with CUDA events on the engine's stream;
+ * lmm_engine_kernel_time waits for the last call and returns both, in ms
+ * (the reference's phase timers, liborSwaptionGreeks.cpp:250-366). */
+int lmm_engine_set_timing(lmm_engine *e, int32_t enable);
+int lmm_engine_kernel_time(lmm_engine *e, double *main_kernel_ms, double *total_ms);
+
+/* Roofline calibration: sustained FP32 FMA throughput (TFLOP/s, 2 flops per
+ * FMA) of `device`, from a register-resident FMA-chain kernel timed with CUDA
+ * events over about `ms` milliseconds. */
+int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops);
+
+/* ---- value + all Greeks, FP32 adjoint (the fast path) ----------------- */
+/* Replaces the per-path work of liborSwaptionGreeks.cpp:281-344 (forward,
+ * payoff adjoint, reverse sweep) plus the vega adjoint, for every path, with
+ * FP64 cross-path sums. Oracle mode: normals read from memory. */
+int lmm_greeks_f32_host(lmm_engine *e, const float *z, int64_t paths, double *out, double *se);
+int lmm_greeks_f32_device(lmm_engine *e, const float *d_z, int64_t paths, double *d_out,
+                          double *d_se);
+/* Throughput mode: normals generated in-kernel by Philox4x32-10, counter
+ * {n/4, 0, lo32(path0+p), hi32(path0+p)}, key {lo32(seed), hi32(seed)}. */
+int lmm_greeks_philox_host(lmm_engine *e, uint64_t seed, int64_t path0, int64_t paths,
+                           double *out, double *se);
+int lmm_greeks_philox_device(lmm_engine *e, uint64_t seed, int64_t path0, int64_t paths,
+                             double *d_out, double *d_se);
+
+/* ---- forward/backward pair (same arithmetic as the fused call) ------- */
+/* The tape holds, per path, the terminal rates and the per-step drift sums
+ * the reverse sweep restarts from: (nn + nmat) floats. */
+int lmm_tape_create(lmm_engine *e, int64_t paths, lmm_tape **out);
+int lmm_tape_destroy(lmm_tape *t);
+/* Forward: value per scenario (d_value[nscen], d_value_se[nscen] or NULL). */
+int lmm_forward_f32_device(lmm_engine *e, const float *d_z, int64_t paths, lmm_tape *t,
+                           double *d_value, double *d_value_se);
+/* Backward: value_bar[nscen] (host) is the upstream gradient of each value;
+ * d_grad[s*2nn + i] = value_bar[s] * dV_s/dL0[i], d_grad[s*2nn + nn + k] =
+ * value_bar[s] * dV_s/dlambda[k]. d_grad_se (or NULL): their standard errors. */
+int lmm_backward_f32_device(lmm_engine *e, const float *d_z, const lmm_tape *t,
+                            const double *value_bar, double *d_grad, double *d_grad_se);
+
+/* ---- FP64 paths (oracle mode and the bump-and-revalue comparator) ---- */
+/* Same outputs as lmm_greeks_f32_*, computed in FP64 end to end. */
+int lmm_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double *out, double *se);
+int lmm_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, double *d_out,
+                          double *d_se);
+/* FP64 forward only, re-run with bumped inputs: one-sided differences
+ * (V(theta + h e_j) - V(theta)) / h for the nn L0[i] and the nn lambda[k];
+ * out/se layout as above (se is the standard error of the value only; the
+ * Greek entries of se are 0). This is the plain bump-and-revalue method. */
+int lmm_bump_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, double h,
+                               double *d_out, double *d_se);
+int lmm_bump_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double h,
+                             double *out, double *se);
+
+/* ---- normals ---------------------------------------------------------- */
+/* z[p*nmat+n] for paths path0..path0+paths-1, the same numbers the Philox
+ * mode consumes in-kernel (FP32 spec). Enqueued on `stream`. */
+int lmm_normals_f32_device(uint64_t seed, int64_t path0, int64_t paths, int32_t nmat,
+                           float *d_z, void *stream);
+/* FP64 spec: 32-bit uniforms, FP64 Box-Muller; mean + std_dev * N(0,1). */
+int lmm_normals_f64_device(uint64_t seed, int64_t path0, int64_t paths, int32_t nmat,
+                           double mean, double std_dev, double *d_z, void *stream);
+
+/* ---- the reference's signature ---------------------------------------- */
+/* Drop-in for liborSwaptionGreeks (liborSwaptionGreeks.hpp:12-13) in the
+ * reference's FP64 build (REAL = double, params.h:10-16): fills z[0..num)
+ * with mean + std_dev * N(0,1) from the library's generator (as the
+ * reference refills z through generateRand, :261; like the reference, the
+ * stream is fixed -- key 12345, the reference's default seed, mklRng.h:9 --
+ * and `seed` is accepted and ignored), prices the params.h portfolio on the
+ * :269-271 curve (L0 = 0.051, lambda = 0.2) in FP64 on the GPU, and writes
+ * the MC mean value to *d_v and the MC mean dV/dL0[NN-1] to *d_Lb.
+ * Difference: the reference repeats its whole Monte Carlo NLOOPS = 10 times
+ * and divides by numPaths only (:27,:278,:355-356), so its outputs are
+ * 10x these means. num must equal 40*numPaths. Uses device 0. */
+int lmm_swaption_greeks(double *z, int num, double mean, double std_dev, int seed,
+                        double *d_v, double *d_Lb, int numPaths);
+/* The same for the reference's FP32 build (REAL = float, params.h:17-24),
+ * computed with the FP32 adjoint kernels. */
+int lmm_swaption_greeks_f32(float *z, int num, float mean, float std_dev, int seed,
+                            float *d_v, float *d_Lb, int numPaths);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LMM_GB300_H */

@@ -1,0 +1,247 @@
+"""GPU parity: the CUDA kernels, called through the C-ABI, against the oracle
+on identical normals.
+
+Tolerances:
+  FP64 kernels: relative 1e-12 per output (value, every delta, every vega).
+  FP32 adjoint: per Greek |gpu - oracle| <= 1e-4 * max(|oracle|, 1e-2 * max|group|),
+                groups = {value}, {deltas}, {vegas}; i.e. relative 1e-4, with
+                Greeks below 1% of their group's largest measured against
+                that 1% (their absolute FP32 rounding does not shrink with them).
+"""
+import numpy as np
+import pytest
+
+from conftest import cfgs, pkg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL_F32 = 1e-4
+RTOL_F64 = 1e-12
+
+
+def scaled_err(gpu, ref, nn):
+    gpu, ref = np.asarray(gpu, dtype=np.float64), np.asarray(ref, dtype=np.float64)
+    out = np.zeros_like(ref)
+    for sl in (slice(0, 1), slice(1, 1 + nn), slice(1 + nn, 1 + 2 * nn)):
+        g, r = gpu[sl], ref[sl]
+        floor = 1e-2 * np.max(np.abs(r)) if r.size > 1 else 0.0
+        den = np.maximum(np.abs(r), floor)
+        den = np.where(den > 0, den, 1.0)
+        out[sl] = np.abs(g - r) / den
+    return out
+
+
+def assert_f32_close(gpu, ref, nn, label=""):
+    e = scaled_err(gpu, ref, nn)
+    worst = int(np.argmax(e))
+    print(f"{label} FP32 vs FP64 oracle: max scaled err {e.max():.3e} at output {worst} "
+          f"(value {e[0]:.2e}, deltas {e[1:1 + nn].max():.2e}, vegas {e[1 + nn:].max():.2e})")
+    assert e.max() <= RTOL_F32, (worst, gpu[worst], ref[worst])
+
+
+@pytest.fixture(scope="module")
+def P():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return pkg()
+
+
+def test_fp64_kernel_matches_oracle_1e12(P):
+    cfg = cfgs().workload(1, 2048)
+    z = O.normals_f64(101, cfg.paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        g, gse = e.greeks_f64(z)
+        assert e.last_launches == 2
+    m, se = O.greeks(cfg, z)
+    np.testing.assert_allclose(g[0], m, rtol=RTOL_F64, atol=1e-13 * np.abs(m).max())
+    np.testing.assert_allclose(gse[0], se, rtol=1e-6)
+
+
+def test_fp64_kernel_long_tenor_and_vol_vector(P):
+    for cfg in (cfgs().workload(3, 64), cfgs().workload(4, 256)):
+        z = O.normals_f64(7, cfg.paths, cfg.nmat)
+        with P.Engine(cfg) as e:
+            g, _ = e.greeks_f64(z)
+        m, _ = O.greeks(cfg, z)
+        np.testing.assert_allclose(g[0], m, rtol=1e-11, atol=1e-12 * np.abs(m).max())
+
+
+def test_reference_signature_fp64_drop_in(P):
+    """lmm_swaption_greeks: normals written back into z, value and dV/dL0[79]
+    equal the reference's (NLOOPS-divided) outputs on that z."""
+    num_paths = 512
+    z, d_v, d_lb = P.swaption_greeks(num_paths, 0.0, 1.0, seed=1234)
+    z_ref = O.normals_f64(12345, num_paths, 40)
+    np.testing.assert_allclose(z, z_ref, rtol=1e-13, atol=1e-13)
+    cfg = cfgs().reference_params(num_paths)
+    m, _ = O.greeks(cfg, z)
+    assert d_v == pytest.approx(m[0], rel=RTOL_F64)
+    assert d_lb == pytest.approx(m[cfg.nn], rel=RTOL_F64)
+    # seed is ignored, as in the reference
+    z2, d_v2, _ = P.swaption_greeks(num_paths, 0.0, 1.0, seed=99)
+    assert d_v2 == d_v and np.array_equal(z2, z)
+
+
+def test_reference_signature_fp32_drop_in(P):
+    num_paths = 1024
+    z, d_v, d_lb = P.swaption_greeks_f32(num_paths)
+    cfg = cfgs().reference_params(num_paths)
+    m, _ = O.greeks(cfg, z.astype(np.float64))
+    assert d_v == pytest.approx(m[0], rel=RTOL_F32)
+    assert d_lb == pytest.approx(m[cfg.nn], rel=RTOL_F32)
+
+
+@pytest.mark.parametrize("wl", [1, 4])
+def test_fp32_adjoint_matches_oracle(P, wl):
+    cfg = cfgs().workload(wl, 8192)
+    z = O.normals_f32(2024 + wl, cfg.paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        g, gse = e.greeks_f32(z)
+    m, se = O.greeks(cfg, z.astype(np.float64))
+    assert_f32_close(g[0], m, cfg.nn, f"workload {wl}")
+    np.testing.assert_allclose(gse[0], se, rtol=2e-3, atol=1e-6 * np.abs(se).max())
+    assert g[0][-1] == 0.0                      # vega[NN-1]: lambda[NN-1] is never read
+
+
+def test_fp32_philox_mode_matches_oracle_on_same_counters(P):
+    cfg = cfgs().workload(4, 4096)
+    seed, path0 = 0x1234_5678_9ABC, 1_000_003
+    z = O.normals_f32(seed, cfg.paths, cfg.nmat, path0=path0)
+    with P.Engine(cfg) as e:
+        g, _ = e.greeks_philox(seed, cfg.paths, path0=path0)
+        g2, _ = e.greeks_f32(z)
+    m, _ = O.greeks(cfg, z.astype(np.float64))
+    assert_f32_close(g[0], m, cfg.nn, "philox")
+    # in-kernel normals vs the same normals read from memory: same kernels
+    np.testing.assert_allclose(g[0], g2[0], rtol=2e-6, atol=1e-7 * np.abs(g2).max())
+
+
+def test_device_normals_match_oracle_spec(P):
+    import torch
+    n, nmat, seed = 3000, 40, 77
+    d32 = torch.empty(n * nmat, dtype=torch.float32, device="cuda")
+    d64 = torch.empty(n * nmat, dtype=torch.float64, device="cuda")
+    P.normals_f32_device(seed, n, nmat, d32.data_ptr(), path0=5)
+    P.normals_f64_device(seed, n, nmat, d64.data_ptr(), path0=5)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(d32.cpu().numpy(), O.normals_f32(seed, n, nmat, path0=5), rtol=0, atol=4e-6)
+    np.testing.assert_allclose(d64.cpu().numpy(), O.normals_f64(seed, n, nmat, path0=5), rtol=0, atol=1e-13)
+
+
+def test_forward_backward_pair_equals_fused(P):
+    import torch
+    cfg = cfgs().workload(4, 3000)
+    z = O.normals_f32(5, cfg.paths, cfg.nmat)
+    dz = torch.from_numpy(z).cuda()
+    with P.Engine(cfg) as e:
+        fused, _ = e.greeks_f32(z)
+        t = e.tape(cfg.paths)
+        val = torch.zeros(1, dtype=torch.float64, device="cuda")
+        grad = torch.zeros(2 * cfg.nn, dtype=torch.float64, device="cuda")
+        e.forward_f32_device(dz.data_ptr(), cfg.paths, t, val.data_ptr())
+        e.backward_f32_device(dz.data_ptr(), t, [2.5], grad.data_ptr())
+        e.synchronize()
+        t.close()
+    f = fused[0]
+    assert val.item() == pytest.approx(f[0], rel=1e-12)
+    np.testing.assert_allclose(grad.cpu().numpy(), 2.5 * f[1:], rtol=2e-6, atol=1e-6 * np.abs(f[1:]).max())
+
+
+def test_bump_comparator_matches_oracle_bumped_values(P):
+    cfg = cfgs().workload(1, 512)
+    z = O.normals_f64(9, cfg.paths, cfg.nmat)
+    h = 1e-6
+    with P.Engine(cfg) as e:
+        g, _ = e.bump_greeks_f64(z, h)
+        assert e.last_launches == 3
+    base, _ = O.value(cfg, z)
+    assert g[0][0] == pytest.approx(base, rel=RTOL_F64)
+    for i in (0, 17, 45, 79):
+        L0 = cfg.L0.copy(); L0[i] += h
+        up, _ = O.value(cfg, z, L0=L0)
+        lam = cfg.lam.copy(); lam[i] += h
+        upl, _ = O.value(cfg, z, lam=lam)
+        assert g[0][1 + i] == pytest.approx((up - base) / h, rel=1e-6, abs=1e-6)
+        assert g[0][1 + cfg.nn + i] == pytest.approx((upl - base) / h, rel=1e-6, abs=1e-6)
+
+
+def test_scenarios_equal_separate_runs(P):
+    base = cfgs().workload(5, 1500)
+    cfg = base.with_paths(1500)
+    cfg.L0 = base.L0[:3].copy()
+    z = O.normals_f32(11, cfg.paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        g, _ = e.greeks_f32(z)
+    assert g.shape == (3, cfg.nout)
+    for s in range(3):
+        one = cfg.scenario(s)
+        with P.Engine(one) as e1:
+            g1, _ = e1.greeks_f32(z)
+        np.testing.assert_allclose(g[s], g1[0], rtol=1e-6, atol=1e-7 * np.abs(g1).max())
+        m, _ = O.greeks(one, z.astype(np.float64))
+        assert_f32_close(g[s], m, one.nn, f"scenario {s}")
+
+
+def test_deterministic_bitwise(P):
+    cfg = cfgs().workload(1, 5000)
+    z = O.normals_f32(3, cfg.paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        a, _ = e.greeks_f32(z)
+        b, _ = e.greeks_f32(z)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("paths", [1, 31, 33, 129, 1000])
+def test_ragged_path_counts(P, paths):
+    cfg = cfgs().workload(4, paths)
+    z = O.normals_f32(8, paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        g, _ = e.greeks_f32(z)
+        g64, _ = e.greeks_f64(z.astype(np.float64))
+    m, _ = O.greeks(cfg, z.astype(np.float64))
+    np.testing.assert_allclose(g64[0], m, rtol=1e-11, atol=1e-12 * np.abs(m).max())
+    assert_f32_close(g[0], m, cfg.nn, f"{paths} paths")
+
+
+def test_error_statuses(P):
+    cfg = cfgs().workload(1, 64)
+    z = O.normals_f32(1, 64, 40)
+    with P.Engine(cfg) as e:
+        with pytest.raises(P.LmmError) as ei:
+            e.greeks_f32(z, paths=0)
+        assert ei.value.code == -1
+        bad = z.copy(); bad[100] = np.nan
+        with pytest.raises(P.LmmError) as ei:
+            e.greeks_f32(bad)
+        assert ei.value.code == -4
+        ok, _ = e.greeks_f32(z)                  # the engine stays usable
+        assert np.all(np.isfinite(ok))
+    bad_cfg = cfgs().workload(1, 64)
+    bad_cfg.maturities = bad_cfg.maturities.copy(); bad_cfg.maturities[0] = 77
+    with pytest.raises(P.LmmError) as ei:
+        P.Engine(bad_cfg)
+    assert ei.value.code == -1
+
+
+def test_full_size_fp32_vs_fp64_on_gpu(P):
+    """Headline size (4,194,304 paths): FP32 adjoint against the GPU FP64
+    kernel (itself pinned to the oracle above) on the identical normals."""
+    import torch
+    cfg = cfgs().workload(2)
+    n = cfg.paths
+    dz = torch.empty(n * cfg.nmat, dtype=torch.float32, device="cuda")
+    P.normals_f32_device(42, n, cfg.nmat, dz.data_ptr())
+    dz64 = dz.double()
+    out32 = torch.zeros(cfg.nout, dtype=torch.float64, device="cuda")
+    se32 = torch.zeros(cfg.nout, dtype=torch.float64, device="cuda")
+    out64 = torch.zeros(cfg.nout, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    with P.Engine(cfg) as e:
+        e.greeks_f32_device(dz.data_ptr(), n, out32.data_ptr(), se32.data_ptr())
+        e.greeks_f64_device(dz64.data_ptr(), n, out64.data_ptr())
+        e.synchronize()
+    g, r, se = out32.cpu().numpy(), out64.cpu().numpy(), se32.cpu().numpy()
+    assert_f32_close(g, r, cfg.nn, "4,194,304 paths")
+    # rounding error far below the Monte Carlo error
+    assert np.all(np.abs(g - r) <= 0.05 * se + 1e-12)
