@@ -182,7 +182,7 @@ def run_ours(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    cfg = P.configs.workload(WORKLOAD)
+    cfg = P.configs.workload(WORKLOAD, args.paths)
     n, nmat, nout = cfg.paths, cfg.nmat, cfg.nout
     stream = torch.cuda.current_stream(dev)
 
@@ -309,10 +309,10 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: Philox4x32-10 + Box-Muller N(0,1), FP32 [4194304 x 40] path-major in HBM",
+            "data": f"synthetic: Philox4x32-10 + Box-Muller N(0,1), FP32 [{n} x {nmat}] path-major in HBM",
             "config": {"workload": cfg.name, "nn": cfg.nn, "nmat": nmat, "paths_per_step": n,
                        "greeks": 2 * cfg.nn, "normals": "HBM, read once per step",
-                       "l2": "inputs larger than L2: 671 MB of normals per step vs 129 MB L2",
+                       "l2": f"inputs larger than L2: {4 * n * nmat / 1e6:.0f} MB of normals per step vs 129 MB L2",
                        "parallelism": f"replicas x{ws} (independent path ranges, no collective)"},
             "gpu_launches": launches,
             "e2e": {"value": e2e, "unit": "paths/s", "h2d_bytes_per_step": 4 * n * nmat,
@@ -335,6 +335,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--paths", type=int, default=None,
+                    help="paths per step (default: the workload's 4,194,304); smaller only for profiling")
     ap.add_argument("--bump-paths", type=int, default=16384)
     ap.add_argument("--cpu-seconds", type=float, default=3.0)
     ap.add_argument("--kernel-times", action="store_true",

@@ -224,6 +224,8 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     if (fam == 0)
         return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for nn=" + std::to_string(e->nn) +
                                              ", nmat=" + std::to_string(e->nmat));
+    if (fam == 2 && mode != Mode::Fused)
+        return fail(LMM_ERR_UNSUPPORTED, "the forward/backward pair covers nn=80, nmat=40 only");
     LMM_TRY(set_device(e));
     int bps = 0;
     LMM_TRY(blocks_per_sm(e, fam, mode, philox, &bps));

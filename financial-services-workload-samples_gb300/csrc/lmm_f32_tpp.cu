@@ -8,29 +8,51 @@
 // registers (the rate index is a compile-time register index; the step index
 // is a runtime loop).
 //
-// The reverse sweep needs, at step n, the pre-step rates L_{n,i}. Instead of
-// storing the NN x NMAT trajectory (9.5 KB per path) it runs the Euler step
-// backwards: with V_i the inclusive drift sum of step n (saved per step in
-// shared memory by the forward), L_{n,i} = L_{n+1,i} * 2^-(a_k (V_i + sqez) + c_k)
-// and V_{i-1} = V_i - delta^2 lambda_k L_{n,i}/(1+delta L_{n,i}), descending in
-// i, which is the order the adjoint needs. In terms of Pb the reference's
+// Branch-free steps. Step n moves rates i > n only. The per-maturity
+// constants are stored with NMAT zero entries in front (k = i-n-1 < 0), so a
+// cell with i <= n multiplies L by 2^0 = 1 and adds 0 to every running sum:
+// it is an exact no-op. Each step is then one straight-line block over rates
+// I0..NN-1 that the compiler can schedule across cells; the steps are split
+// into SEG segments with their own I0 (= first step of the segment + 1) so
+// that only a few no-op cells run per step.
+//
+// Reverse sweep without a stored trajectory. With V_i the inclusive drift sum
+// of step n (saved per step by the forward), the Euler step runs backwards,
+// descending in i as the adjoint needs:
+//   L_{n,i} = L_{n+1,i} * 2^-(a_k (V_i + sqez) + c_k),  V_{i-1} = V_i - delta^2 lambda_k t
+// with t = L/(1+delta L), r = 1/(1+delta L). In terms of Pb the reference's
 // update (:108-111) becomes
-//   S  += lambda_k Pb_i                         (S is the reference's v1)
-//   Pb_i += delta^2 lambda_k t r S,  t = L/(1+delta L), r = 1/(1+delta L)
+//   S += lambda_k Pb_i,   Pb_i += delta^2 lambda_k t r S     (S is the reference's v1)
 // and the vega of cell (n,i), k = i-n-1, is
 //   dV/dlambda_k += Pb_i (V_i + sqez - delta lambda_k) + delta^2 t S.
+// The reconstruction is a serial chain (exp -> rcp -> drift sum) per step, so
+// steps are processed in skewed pairs: cell (n,i) next to cell (n-1,i+1),
+// two independent chains in one instruction stream.
 //
 // Cross-path reduction: per warp, each lane sums one output column over the
 // warp's 32 paths (shared-memory transpose), then adds into per-warp FP64
-// accumulators; each block writes its FP64 partial sums, and lmm_aux.cu adds
-// the partials in a fixed order, so results are bit-reproducible.
+// accumulators; each block writes FP64 partial sums that lmm_aux.cu adds in a
+// fixed order, so results are bit-reproducible.
 #include "lmm_device.cuh"
+
+#ifndef LMM_TPP_BLOCK
+#define LMM_TPP_BLOCK 64
+#endif
+#ifndef LMM_TPP_MINB
+#define LMM_TPP_MINB 4
+#endif
+#ifndef LMM_TPP_SEGF
+#define LMM_TPP_SEGF 8
+#endif
+#ifndef LMM_TPP_SEGR
+#define LMM_TPP_SEGR 4
+#endif
 
 namespace lmm {
 namespace {
 
-constexpr int kTppBlock = 128;
-constexpr int kTppMinBlocks = 3;
+constexpr int kTppBlock = LMM_TPP_BLOCK;
+constexpr int kTppMinBlocks = LMM_TPP_MINB;
 
 __host__ __device__ constexpr int align16(int x) { return (x + 15) & ~15; }
 
@@ -39,29 +61,101 @@ struct TppLayout {
     static constexpr int B = kTppBlock;
     static constexpr int NW = B / 32;
     static constexpr int M = NN - NMAT;
+    static constexpr int PAD = NMAT;                 // k = i-n-1 >= -NMAT
     static constexpr int NOUT = MODE == Mode::Fused ? 1 + 2 * NN : (MODE == Mode::Forward ? 1 : 2 * NN);
-    static constexpr int kc = 0;                                    // float4[NN]
-    static constexpr int kd = kc + 16 * NN;                         // float[NN]
-    static constexpr int l0 = kd + 4 * NN;                          // float[NN]
-    static constexpr int il0 = l0 + 4 * NN;                         // float[NN]
-    static constexpr int ost = il0 + 4 * NN;                        // int[M+1]
-    static constexpr int okf = align16(ost + 4 * (M + 1));          // float[kMaxNopt]
-    static constexpr int okd = align16(okf + 4 * kMaxNopt);         // double[kMaxNopt]
-    static constexpr int vg = align16(okd + 8 * kMaxNopt);          // float[NN][B]
-    static constexpr int vg_bytes = MODE == Mode::Forward ? 0 : 4 * NN * B;
-    static constexpr int vt = vg + vg_bytes;                        // float[NMAT][B]
+    static constexpr int kc = 0;                                     // float4[PAD+NN]
+    static constexpr int kx = kc + 16 * (PAD + NN);                  // float2[PAD+NN]
+    static constexpr int l0 = kx + 8 * (PAD + NN);                   // float[NN]
+    static constexpr int il0 = l0 + 4 * NN;                          // float[NN]
+    static constexpr int ost = il0 + 4 * NN;                         // int[M+1]
+    static constexpr int okf = align16(ost + 4 * (M + 1));           // float[kMaxNopt]
+    static constexpr int okd = align16(okf + 4 * kMaxNopt);          // double[kMaxNopt]
+    static constexpr int vt = align16(okd + 8 * kMaxNopt);           // float[NMAT][B]
     static constexpr int vt_bytes = MODE == Mode::Fused ? 4 * NMAT * B : 0;
-    static constexpr int acc = align16(vt + vt_bytes);              // double[NW][2*NOUT]
+    static constexpr int vg = vt + vt_bytes;                         // float[PAD+NN][B]
+    static constexpr int vg_bytes = MODE == Mode::Forward ? 0 : 4 * (PAD + NN) * B;
+    static constexpr int acc = align16(vg + vg_bytes);               // double[NW][2*NOUT]
     static constexpr int bytes = acc + 8 * NW * 2 * NOUT;
 };
 
-__device__ __forceinline__ float pick4(const float (&q)[4], int j)
+__device__ __forceinline__ float pick4(const float4 &q, int j)
 {
-    float r = q[0];
-    r = j == 1 ? q[1] : r;
-    r = j == 2 ? q[2] : r;
-    r = j == 3 ? q[3] : r;
+    float r = q.x;
+    r = j == 1 ? q.y : r;
+    r = j == 2 ? q.z : r;
+    r = j == 3 ? q.w : r;
     return r;
+}
+
+// Four consecutive normals n = 4q..4q+3 of one path: read from memory (16-byte
+// aligned since nmat % 4 == 0) or generated by Philox.
+template <bool PHILOX, int NMAT>
+__device__ __forceinline__ float4 zquad(const float *zp, uint64_t seed, uint64_t gpath, int q)
+{
+    if (PHILOX) {
+        float g[4];
+        normals_quad_f32(seed, gpath, (uint32_t)q, g);
+        return make_float4(g[0], g[1], g[2], g[3]);
+    } else {
+        return __ldg(reinterpret_cast<const float4 *>(zp) + q);
+    }
+}
+
+// One forward Euler step over rates I0..NN-1 (path_calc_b1 :63-77).
+// kcn[i] holds the constants of k = i-n-1, zero for k < 0.
+template <int NN, int I0>
+__device__ __forceinline__ float fwd_step(float (&L)[NN], const float4 *kcn, float sqez, float delta)
+{
+    float V = 0.0f;
+#pragma unroll
+    for (int i = I0; i < NN; ++i) {
+        const float4 k = kcn[i];
+        const float r = rcp_approx(fmaf(delta, L[i], 1.0f));
+        V = fmaf(k.z, L[i] * r, V);
+        L[i] *= ex2_approx(fmaf(k.x, V + sqez, k.y));
+    }
+    return V;
+}
+
+struct RevStep {
+    float V, S, sqez;
+    const float4 *kc;   // kc[i]: constants of k = i-n-1
+    const float2 *kx;   // kx[i]: {delta*lambda_k, 1}, zero for k < 0
+    float *vg;          // vg[i*B]: this thread's vega slot of k = i-n-1
+};
+
+// One reverse cell (path_calc_b2 :105-111 in log-adjoint form) + vega.
+template <int NN, int B>
+__device__ __forceinline__ void rev_cell(float (&L)[NN], float (&Pb)[NN], RevStep &s, int i,
+                                         float delta, float d2)
+{
+    const float4 k = s.kc[i];
+    const float2 x = s.kx[i];
+    const float y = s.V + s.sqez;
+    const float Ln = L[i] * ex2_approx(-fmaf(k.x, y, k.y));
+    const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
+    const float t = Ln * r;
+    s.V = fmaf(-k.z, t, s.V);
+    const float pb = Pb[i];
+    s.S = fmaf(k.w, pb, s.S);
+    const float tS = t * s.S;
+    float *v = s.vg + i * B;
+    *v += x.y * fmaf(pb, y - x.x, d2 * tS);
+    Pb[i] = fmaf(k.z * r, tS, pb);
+    L[i] = Ln;
+}
+
+// Steps hi = n and lo = n-1 together, skewed by one rate: at position i the
+// cells (hi, i) and (lo, i+1) are independent.
+template <int NN, int B, int I0>
+__device__ __forceinline__ void rev_pair(float (&L)[NN], float (&Pb)[NN], RevStep &hi, RevStep &lo,
+                                         float delta, float d2)
+{
+#pragma unroll
+    for (int i = NN - 1; i >= I0 - 1; --i) {
+        if (i >= I0) rev_cell<NN, B>(L, Pb, hi, i, delta, d2);
+        if (i + 1 <= NN - 1) rev_cell<NN, B>(L, Pb, lo, i + 1, delta, d2);
+    }
 }
 
 // Portfolio value, portfolio_b :133-171 and :186-197. Reciprocals are the
@@ -159,30 +253,104 @@ __device__ __forceinline__ void column_reduce(const float *vg, int warp, int lan
     }
 }
 
+// Forward over all steps, segment by segment (segment s: steps [lo, hi),
+// body over rates lo+1..NN-1).
+template <int NN, int NMAT, int SEG, bool PHILOX, Mode MODE, int S = 0>
+__device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, float4 &zq,
+                                            float4 &zq_next, const float *zp, uint64_t seed,
+                                            uint64_t gpath, float sqd, float delta, float *vt_s,
+                                            float *tape_v, int64_t total, bool active)
+{
+    if constexpr (S < SEG) {
+        constexpr int lo = S * NMAT / SEG, hi = (S + 1) * NMAT / SEG;
+        constexpr int B = kTppBlock;
+        for (int n = lo; n < hi; ++n) {
+            if ((n & 3) == 0) {
+                zq = zq_next;
+                if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+            }
+            const float sqez = sqd * pick4(zq, n & 3);
+            const float V = fwd_step<NN, lo + 1>(L, kc0 - (n + 1), sqez, delta);
+            if (MODE == Mode::Fused)
+                vt_s[n * B] = V;
+            else if (active)
+                tape_v[(int64_t)n * total] = V;
+        }
+        forward_all<NN, NMAT, SEG, PHILOX, MODE, S + 1>(L, kc0, zq, zq_next, zp, seed, gpath, sqd,
+                                                        delta, vt_s, tape_v, total, active);
+    }
+}
+
+// Reverse over all steps, segments from the last, pairs (n, n-1) within each.
+template <int NN, int NMAT, int SEG, bool PHILOX, Mode MODE, int S = SEG - 1>
+__device__ __forceinline__ void reverse_all(float (&L)[NN], float (&Pb)[NN], const float4 *kc0,
+                                            const float2 *kx0, float *vg0, float4 &zq,
+                                            float4 &zq_next, const float *zp, uint64_t seed,
+                                            uint64_t gpath, float sqd, float delta, float d2,
+                                            const float *vt_s, const float *tape_v, int64_t total)
+{
+    if constexpr (S >= 0) {
+        constexpr int lo = S * NMAT / SEG, hi = (S + 1) * NMAT / SEG;
+        static_assert((hi - lo) % 2 == 0, "reverse segments hold whole step pairs");
+        constexpr int B = kTppBlock;
+        for (int n = hi - 1; n > lo; n -= 2) {
+            if ((n & 3) == 3) {
+                zq = zq_next;
+                if ((n >> 2) > 0) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) - 1);
+            }
+            RevStep h, l;
+            h.sqez = sqd * pick4(zq, n & 3);
+            l.sqez = sqd * pick4(zq, (n - 1) & 3);
+            if (MODE == Mode::Fused) {
+                h.V = vt_s[n * B];
+                l.V = vt_s[(n - 1) * B];
+            } else {
+                h.V = tape_v[(int64_t)n * total];
+                l.V = tape_v[(int64_t)(n - 1) * total];
+            }
+            h.S = 0.0f;
+            l.S = 0.0f;
+            h.kc = kc0 - (n + 1);
+            l.kc = kc0 - n;
+            h.kx = kx0 - (n + 1);
+            l.kx = kx0 - n;
+            h.vg = vg0 - (n + 1) * B;
+            l.vg = vg0 - n * B;
+            rev_pair<NN, B, lo + 1>(L, Pb, h, l, delta, d2);
+        }
+        reverse_all<NN, NMAT, SEG, PHILOX, MODE, S - 1>(L, Pb, kc0, kx0, vg0, zq, zq_next, zp, seed,
+                                                        gpath, sqd, delta, d2, vt_s, tape_v, total);
+    }
+}
+
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
 __global__ void __launch_bounds__(kTppBlock, kTppMinBlocks)
 k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
       float *__restrict__ tape, const double *__restrict__ vbar)
 {
     using Lay = TppLayout<NN, NMAT, MODE>;
-    constexpr int B = Lay::B, M = Lay::M, NOUT = Lay::NOUT;
+    constexpr int B = Lay::B, M = Lay::M, NOUT = Lay::NOUT, PAD = Lay::PAD;
+    static_assert(NMAT % 4 == 0, "normals are read in aligned quads");
     extern __shared__ __align__(16) unsigned char smem[];
     float4 *kc_s = reinterpret_cast<float4 *>(smem + Lay::kc);
-    float *kd_s = reinterpret_cast<float *>(smem + Lay::kd);
+    float2 *kx_s = reinterpret_cast<float2 *>(smem + Lay::kx);
     float *l0_s = reinterpret_cast<float *>(smem + Lay::l0);
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
     float *okf_s = reinterpret_cast<float *>(smem + Lay::okf);
     double *okd_s = reinterpret_cast<double *>(smem + Lay::okd);
-    float *vg_s = reinterpret_cast<float *>(smem + Lay::vg);
     float *vt_s = reinterpret_cast<float *>(smem + Lay::vt);
+    float *vg_s = reinterpret_cast<float *>(smem + Lay::vg);
     double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int scen = blockIdx.x / w.items, item = blockIdx.x % w.items;
+    for (int i = tid; i < PAD + NN; i += B) {
+        const int k = i - PAD;
+        kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
+        kx_s[i] = k < 0 ? make_float2(0.f, 0.f) : make_float2(m.kd[k], 1.0f);
+    }
     for (int i = tid; i < NN; i += B) {
-        kc_s[i] = m.kc[i];
-        kd_s[i] = m.kd[i];
         l0_s[i] = m.L0f[scen * NN + i];
         il0_s[i] = m.invL0f[scen * NN + i];
     }
@@ -199,49 +367,31 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     const int64_t total = (int64_t)m.nscen * w.paths;
     const int64_t ibase = (int64_t)item * w.ppt * B;
     const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
+    const float4 *kc0 = kc_s + PAD;
+    const float2 *kx0 = kx_s + PAD;
+    float *vg0 = vg_s + PAD * B + tid;
+    float *vt0 = vt_s + tid;
 
     for (int j = 0; j < w.ppt; ++j) {
+        if (ibase + (int64_t)j * B >= w.paths) break;          // block-uniform
         const int64_t pl = ibase + (int64_t)j * B + tid;
-        if (ibase + (int64_t)j * B >= w.paths) break;          // warp-uniform: whole batch past the end
         const bool active = pl < w.paths;
         const int64_t pc = active ? pl : w.paths - 1;
         const int64_t tp = (int64_t)scen * w.paths + pc;
         const float *zp = PHILOX ? nullptr : z + pc * NMAT;
         const uint64_t gpath = (uint64_t)(path0 + pc);
+        float *tape_v = tape ? tape + (int64_t)NN * total + tp : nullptr;
 
         float L[NN];
         float Pb[NN];
-        float zq[4];
-        double V = 0.0, disc = 1.0, bM = 1.0;
-        unsigned long long mask = 0ull;
+        float4 zq, zq_next;
 
         if (MODE != Mode::Backward) {
 #pragma unroll
             for (int i = 0; i < NN; ++i) L[i] = l0_s[i];
-            for (int n = 0; n < NMAT; ++n) {
-                float zn;
-                if (PHILOX) {
-                    if ((n & 3) == 0) normals_quad_f32(seed, gpath, (uint32_t)(n >> 2), zq);
-                    zn = pick4(zq, n & 3);
-                } else {
-                    zn = __ldg(zp + n);
-                }
-                const float sqez = sqd * zn;
-                float Vs = 0.0f;
-#pragma unroll
-                for (int i = 1; i < NN; ++i) {
-                    if (i > n) {
-                        const float4 k = kc_s[i - n - 1];
-                        const float r = rcp_approx(fmaf(delta, L[i], 1.0f));
-                        Vs = fmaf(k.z, L[i] * r, Vs);
-                        L[i] *= ex2_approx(fmaf(k.x, Vs + sqez, k.y));
-                    }
-                }
-                if (MODE == Mode::Fused)
-                    vt_s[n * B + tid] = Vs;
-                else if (active)
-                    tape[(int64_t)(NN + n) * total + tp] = Vs;
-            }
+            zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
+            forward_all<NN, NMAT, LMM_TPP_SEGF, PHILOX, MODE>(L, kc0, zq, zq_next, zp, seed, gpath, sqd,
+                                                              delta, vt0, tape_v, total, active);
             if (MODE == Mode::Forward && active) {
 #pragma unroll
                 for (int i = 0; i < NN; ++i) tape[(int64_t)i * total + tp] = L[i];
@@ -251,42 +401,17 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             for (int i = 0; i < NN; ++i) L[i] = tape[(int64_t)i * total + tp];
         }
 
-        V = payoff_forward<NN, NMAT>(L, delta, ost_s, okd_s, &disc, &bM, &mask);
+        double disc = 1.0, bM = 1.0;
+        unsigned long long mask = 0ull;
+        const double V = payoff_forward<NN, NMAT>(L, delta, ost_s, okd_s, &disc, &bM, &mask);
 
         if (MODE != Mode::Forward) {
             payoff_adjoint<NN, NMAT>(L, Pb, vb, V, disc, bM, mask, delta, ost_s, okf_s);
 #pragma unroll
-            for (int k = 0; k < NN; ++k) vg_s[k * B + tid] = 0.0f;
-            for (int n = NMAT - 1; n >= 0; --n) {
-                float zn;
-                if (PHILOX) {
-                    if ((n & 3) == 3 || n == NMAT - 1) normals_quad_f32(seed, gpath, (uint32_t)(n >> 2), zq);
-                    zn = pick4(zq, n & 3);
-                } else {
-                    zn = __ldg(zp + n);
-                }
-                const float sqez = sqd * zn;
-                float Vs = MODE == Mode::Fused ? vt_s[n * B + tid] : tape[(int64_t)(NN + n) * total + tp];
-                float S = 0.0f;
-#pragma unroll
-                for (int i = NN - 1; i >= 1; --i) {
-                    if (i > n) {
-                        const int kk = i - n - 1;
-                        const float4 k = kc_s[kk];
-                        const float y = Vs + sqez;
-                        const float Ln = L[i] * ex2_approx(-fmaf(k.x, y, k.y));
-                        const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
-                        const float t = Ln * r;
-                        Vs = fmaf(-k.z, t, Vs);
-                        const float pb = Pb[i];
-                        S = fmaf(k.w, pb, S);
-                        const float tS = t * S;
-                        vg_s[kk * B + tid] += fmaf(pb, y - kd_s[kk], d2 * tS);
-                        Pb[i] = fmaf(k.z * r, tS, pb);
-                        L[i] = Ln;
-                    }
-                }
-            }
+            for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+            zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);
+            reverse_all<NN, NMAT, LMM_TPP_SEGR, PHILOX, MODE>(L, Pb, kc0, kx0, vg0, zq, zq_next, zp, seed,
+                                                              gpath, sqd, delta, d2, vt0, tape_v, total);
         }
 
         // ---- cross-path reduction of this batch of B paths ----
@@ -301,17 +426,18 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         if (MODE != Mode::Forward) {
             constexpr int voff = MODE == Mode::Fused ? 1 + NN : NN;
             constexpr int doff = MODE == Mode::Fused ? 1 : 0;
+            float *vgw = vg_s + PAD * B;
             if (!active) {
 #pragma unroll
-                for (int k = 0; k < NN; ++k) vg_s[k * B + tid] = 0.0f;
+                for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
             }
             __syncwarp();
-            column_reduce<NN, B>(vg_s, warp, lane, acc, NOUT, voff);
+            column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, voff);
             __syncwarp();
 #pragma unroll
-            for (int i = 0; i < NN; ++i) vg_s[i * B + tid] = active ? Pb[i] * il0_s[i] : 0.0f;
+            for (int i = 0; i < NN; ++i) vg0[i * B] = active ? Pb[i] * il0_s[i] : 0.0f;
             __syncwarp();
-            column_reduce<NN, B>(vg_s, warp, lane, acc, NOUT, doff);
+            column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, doff);
             __syncwarp();
         }
     }

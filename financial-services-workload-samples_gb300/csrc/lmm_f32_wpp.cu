@@ -1,18 +1,428 @@
-// FP32 warp-per-path LMM kernels for shapes other than NN=80/NMAT=40.
+// FP32 warp-per-path LMM kernels: any NN <= 256 (long tenor, e.g. NN=160,
+// NMAT=120), reverse sweep recomputed from checkpoints.
+//
+// One warp carries one Monte Carlo path. Lane l holds the S consecutive rates
+// i = S*l + s (s < S) in registers, so
+//   - the drift sum of path_calc_b1 (LiborMarketModel/liborSwaptionGreeks.cpp:70),
+//     an inclusive prefix sum over i, is a local prefix over the lane's slots
+//     plus an exclusive warp scan of the lane totals (shuffles);
+//   - the reverse running sum v1 of path_calc_b2 (:108), a suffix sum over i,
+//     is the mirror image (local suffix + exclusive warp suffix scan).
+// The forward stores the rates every kWppCkpt steps in shared memory. The
+// reverse sweep restores each checkpoint, recomputes its kWppCkpt steps
+// keeping t = L/(1+delta L) and the drift sums of every cell in registers,
+// then runs the adjoint of those steps backwards (Pb = L dV/dL, the
+// log-adjoint):
+//   S_i = sum_{j>=i} lambda_k Pb_j,  Pb_i += delta^2 lambda_k t r S_i,  r = 1 - delta t
+//   dV/dlambda_k += Pb_i (V_i + sqez - delta lambda_k) + delta^2 t S_i.
+// The payoff (portfolio_b :120-211, aliasing fixed) runs with FP64 products:
+// the discount product is a warp product reduction, the annuity recursion
+// runs on lane 0.
 #include "lmm_device.cuh"
 
 namespace lmm {
+namespace {
 
-bool f32_wpp_supports(int, int) { return false; }
-int wpp_block_threads() { return 128; }
-cudaError_t wpp_blocks_per_sm(int, int, Mode, bool, int *blocks)
+constexpr int kWppBlock = 128;
+constexpr int kWppWarps = kWppBlock / 32;
+constexpr int kWppCkpt = 8;
+
+__host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// Shared-memory layout (bytes), shared by host and device.
+struct WppLay {
+    int nn, nmat, S, nck, nout, M;
+    size_t kc, kd, l0, il0, ost, okf, okd, warp0, per_warp, ck, vg, lw, acc, bytes;
+};
+
+__host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
+{
+    WppLay L{};
+    L.nn = nn;
+    L.nmat = nmat;
+    L.S = S;
+    L.M = nn - nmat;
+    L.nck = (nmat + kWppCkpt - 1) / kWppCkpt;
+    L.nout = 1 + 2 * nn;
+    size_t o = 0;
+    L.kc = o; o = al16(o + 16 * (size_t)nn);
+    L.kd = o; o = al16(o + 4 * (size_t)nn);
+    L.l0 = o; o = al16(o + 4 * (size_t)nn);
+    L.il0 = o; o = al16(o + 4 * (size_t)nn);
+    L.ost = o; o = al16(o + 4 * (size_t)(L.M + 1));
+    L.okf = o; o = al16(o + 4 * (size_t)kMaxNopt);
+    L.okd = o; o = al16(o + 8 * (size_t)kMaxNopt);
+    L.warp0 = o;
+    size_t w = 0;
+    L.ck = w; w = al16(w + 4 * (size_t)L.nck * 32 * S);   // checkpoints [nck][32*S]
+    L.vg = w; w = al16(w + 4 * (size_t)32 * S);           // vegas [32*S] (index k)
+    L.lw = w; w = al16(w + 4 * (size_t)32 * S);           // payoff staging [32*S]
+    L.acc = w; w = al16(w + 8 * (size_t)2 * L.nout);      // FP64 sums [2*nout]
+    L.per_warp = w;
+    L.bytes = o + kWppWarps * w;
+    return L;
+}
+
+__device__ __forceinline__ float warp_excl_prefix(float x, int lane)
+{
+    float inc = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const float y = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += y;
+    }
+    return inc - x;
+}
+
+__device__ __forceinline__ float warp_excl_suffix(float x, int lane)
+{
+    float inc = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const float y = __shfl_down_sync(0xffffffffu, inc, d);
+        if (lane + d < 32) inc += y;
+    }
+    return inc - x;
+}
+
+// One forward step n over the lane's slots. If T/Vs are given, the cell's t
+// and inclusive drift sum are kept (for the recompute of a checkpoint segment).
+template <int S>
+__device__ __forceinline__ void wpp_fwd_step(float (&L)[S], int n, float sqez, int lane, int nn,
+                                             const float4 *kc, float delta, float (*T), float (*Vs))
+{
+    float a[S], t[S];
+    float4 kk[S];
+    float P = 0.0f;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int i = S * lane + s;
+        const bool act = i > n && i < nn;
+        kk[s] = kc[act ? i - n - 1 : 0];
+        const float r = rcp_approx(fmaf(delta, L[s], 1.0f));
+        t[s] = L[s] * r;
+        a[s] = act ? kk[s].z * t[s] : 0.0f;
+        P += a[s];
+        a[s] = P;                                   // local inclusive prefix
+    }
+    const float X = warp_excl_prefix(P, lane);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int i = S * lane + s;
+        const bool act = i > n && i < nn;
+        const float V = X + a[s];
+        if (act) L[s] *= ex2_approx(fmaf(kk[s].x, V + sqez, kk[s].y));
+        if (T) {
+            T[s] = t[s];
+            Vs[s] = V;
+        }
+    }
+}
+
+// Adjoint of step n (path_calc_b2 :100-112 in log-adjoint form) + vega.
+template <int S>
+__device__ __forceinline__ void wpp_rev_step(float (&Pb)[S], int n, float sqez, int lane, int nn,
+                                             const float4 *kc, const float *kd, float *vg,
+                                             const float *T, const float *Vs, float delta, float d2)
+{
+    float b[S];
+    float Q = 0.0f;
+#pragma unroll
+    for (int s = S - 1; s >= 0; --s) {
+        const int i = S * lane + s;
+        const bool act = i > n && i < nn;
+        const float lam = act ? kc[i - n - 1].w : 0.0f;
+        Q = fmaf(lam, Pb[s], Q);
+        b[s] = Q;                                   // local inclusive suffix
+    }
+    const float Y = warp_excl_suffix(Q, lane);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int i = S * lane + s;
+        if (i > n && i < nn) {
+            const int k = i - n - 1;
+            const float4 kk = kc[k];
+            const float Ssum = Y + b[s];
+            const float t = T[s];
+            const float r = fmaf(-delta, t, 1.0f);
+            const float tS = t * Ssum;
+            vg[k] += fmaf(Pb[s], Vs[s] + sqez - kd[k], d2 * tS);
+            Pb[s] = fmaf(kk.z * r, tS, Pb[s]);
+        }
+    }
+}
+
+template <bool PHILOX>
+struct ZChunk {
+    // Normals of steps 32q..32q+31 of one path spread over the warp: lane l
+    // holds step 32q+l (memory) or steps 32q+4l..+3 (Philox, lanes < 8).
+    float v[4];
+    int q = -1;
+    __device__ __forceinline__ void load(int qq, const float *zp, int nmat, uint64_t seed,
+                                         uint64_t gpath, int lane)
+    {
+        q = qq;
+        if (PHILOX) {
+            const int quad = 8 * qq + lane;
+            if (lane < 8 && 4 * quad < nmat) normals_quad_f32(seed, gpath, (uint32_t)quad, v);
+        } else {
+            const int n = 32 * qq + lane;
+            v[0] = n < nmat ? __ldg(zp + n) : 0.0f;
+        }
+    }
+    __device__ __forceinline__ float get(int n, const float *zp, int nmat, uint64_t seed,
+                                         uint64_t gpath, int lane)
+    {
+        if ((n >> 5) != q) load(n >> 5, zp, nmat, seed, gpath, lane);
+        if (PHILOX) {
+            const int j = n & 3;
+            float x = v[0];
+            x = j == 1 ? v[1] : x;
+            x = j == 2 ? v[2] : x;
+            x = j == 3 ? v[3] : x;
+            return __shfl_sync(0xffffffffu, x, (n & 31) >> 2);
+        }
+        return __shfl_sync(0xffffffffu, v[0], n & 31);
+    }
+};
+
+template <int S, bool PHILOX>
+__global__ void __launch_bounds__(kWppBlock, 3)
+k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nn = m.nn, nmat = m.nmat;
+    const WppLay Ly = wpp_layout(nn, nmat, S);
+    const int M = Ly.M, nout = Ly.nout;
+    float4 *kc_s = reinterpret_cast<float4 *>(smem + Ly.kc);
+    float *kd_s = reinterpret_cast<float *>(smem + Ly.kd);
+    float *l0_s = reinterpret_cast<float *>(smem + Ly.l0);
+    float *il0_s = reinterpret_cast<float *>(smem + Ly.il0);
+    int *ost_s = reinterpret_cast<int *>(smem + Ly.ost);
+    float *okf_s = reinterpret_cast<float *>(smem + Ly.okf);
+    double *okd_s = reinterpret_cast<double *>(smem + Ly.okd);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned char *wbase = smem + Ly.warp0 + warp * Ly.per_warp;
+    float *ck_s = reinterpret_cast<float *>(wbase + Ly.ck);
+    float *vg_s = reinterpret_cast<float *>(wbase + Ly.vg);
+    float *lw_s = reinterpret_cast<float *>(wbase + Ly.lw);
+    double *acc = reinterpret_cast<double *>(wbase + Ly.acc);
+
+    const int scen = blockIdx.x / w.items, item = blockIdx.x % w.items;
+    for (int i = tid; i < nn; i += kWppBlock) {
+        kc_s[i] = m.kc[i];
+        kd_s[i] = m.kd[i];
+        l0_s[i] = m.L0f[scen * nn + i];
+        il0_s[i] = m.invL0f[scen * nn + i];
+    }
+    for (int i = tid; i <= M; i += kWppBlock) ost_s[i] = m.opt_start[i];
+    for (int i = tid; i < m.nopt; i += kWppBlock) {
+        okf_s[i] = m.optKf[i];
+        okd_s[i] = m.optKd[i];
+    }
+    for (int i = lane; i < 2 * nout; i += 32) acc[i] = 0.0;
+    for (int i = lane; i < 32 * S; i += 32) vg_s[i] = 0.0f;
+    __syncthreads();
+
+    const float delta = m.delta, sqd = m.sqd, d2 = m.d2;
+    const int64_t ibase = (int64_t)item * w.ppt * kWppWarps;
+    for (int j = 0; j < w.ppt; ++j) {
+        const int64_t p = ibase + (int64_t)j * kWppWarps + warp;
+        if (p >= w.paths) break;                                  // warp-uniform
+        const float *zp = PHILOX ? nullptr : z + p * nmat;
+        const uint64_t gpath = (uint64_t)(path0 + p);
+        ZChunk<PHILOX> zc;
+
+        float L[S], Pb[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const int i = S * lane + s;
+            L[s] = i < nn ? l0_s[i] : 1.0f;
+        }
+        // ---- forward with checkpoints ----
+        for (int n = 0; n < nmat; ++n) {
+            if (n % kWppCkpt == 0) {
+#pragma unroll
+                for (int s = 0; s < S; ++s) ck_s[(n / kWppCkpt) * 32 * S + S * lane + s] = L[s];
+            }
+            const float sqez = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
+            wpp_fwd_step<S>(L, n, sqez, lane, nn, kc_s, delta, nullptr, nullptr);
+        }
+        // ---- payoff (FP64 products) and its adjoint ----
+        double dprod = 1.0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const int i = S * lane + s;
+            if (i < nmat) dprod *= (double)__frcp_rn(fmaf(delta, L[s], 1.0f));
+            if (i < nn) lw_s[i] = L[s];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dprod *= __shfl_xor_sync(0xffffffffu, dprod, o);
+        const double disc = dprod;
+        __syncwarp();
+        double V = 0.0;
+        if (lane == 0) {
+            double bb = 1.0, ss = 0.0, vs = 0.0;
+            unsigned long long mask = 0ull;
+            for (int mm = 0; mm < M; ++mm) {
+                bb *= (double)__frcp_rn(fmaf(delta, lw_s[nmat + mm], 1.0f));
+                ss = fma((double)delta, bb, ss);
+                for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
+                    const double sw = fma(okd_s[o], ss, bb) - 1.0;
+                    if (sw < 0.0) {
+                        vs -= 100.0 * sw;
+                        mask |= 1ull << o;
+                    }
+                }
+            }
+            V = disc * vs;
+            // :173-184 with the rate kept apart from its adjoint; lw_s[i] becomes
+            // the log-adjoint of rate i >= nmat.
+            const float scale = -(float)disc * delta;
+            float Bm = (float)bb, Sb = 0.0f, Bb = 0.0f;
+            for (int mm = M - 1; mm >= 0; --mm) {
+                const float Ln = lw_s[nmat + mm];
+                const float den = fmaf(delta, Ln, 1.0f);
+                const float r = __frcp_rn(den);
+                for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
+                    if ((mask >> o) & 1ull) {
+                        Sb -= 100.0f * okf_s[o];
+                        Bb -= 100.0f;
+                    }
+                }
+                Bb = fmaf(delta, Sb, Bb);
+                lw_s[nmat + mm] = scale * Bb * Bm * (Ln * r);
+                Bb *= r;
+                Bm *= den;
+            }
+        }
+        V = __shfl_sync(0xffffffffu, V, 0);
+        __syncwarp();
+        const float vsd = -(float)V * delta;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const int i = S * lane + s;
+            if (i < nmat) Pb[s] = vsd * (L[s] * __frcp_rn(fmaf(delta, L[s], 1.0f)));
+            else Pb[s] = i < nn ? lw_s[i] : 0.0f;
+        }
+        // ---- reverse, one checkpoint segment at a time ----
+        for (int c = Ly.nck - 1; c >= 0; --c) {
+#pragma unroll
+            for (int s = 0; s < S; ++s) L[s] = ck_s[c * 32 * S + S * lane + s];
+            float T[kWppCkpt][S], Vs[kWppCkpt][S], zs[kWppCkpt];
+#pragma unroll
+            for (int jj = 0; jj < kWppCkpt; ++jj) {
+                const int n = c * kWppCkpt + jj;
+                if (n < nmat) {
+                    zs[jj] = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
+                    wpp_fwd_step<S>(L, n, zs[jj], lane, nn, kc_s, delta, T[jj], Vs[jj]);
+                }
+            }
+#pragma unroll
+            for (int jj = kWppCkpt - 1; jj >= 0; --jj) {
+                const int n = c * kWppCkpt + jj;
+                if (n < nmat) wpp_rev_step<S>(Pb, n, zs[jj], lane, nn, kc_s, kd_s, vg_s, T[jj], Vs[jj], delta, d2);
+            }
+        }
+        // ---- accumulate this path: value, deltas, vegas ----
+        __syncwarp();
+        if (lane == 0) {
+            acc[0] += V;
+            acc[nout] += V * V;
+        }
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const int i = S * lane + s;
+            if (i < nn) {
+                const double dl = (double)(Pb[s] * il0_s[i]);
+                acc[1 + i] += dl;
+                acc[nout + 1 + i] += dl * dl;
+            }
+        }
+        for (int k = lane; k < nn; k += 32) {
+            const double vgk = (double)vg_s[k];
+            acc[1 + nn + k] += vgk;
+            acc[nout + 1 + nn + k] += vgk * vgk;
+            vg_s[k] = 0.0f;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int o = tid; o < 2 * nout; o += kWppBlock) {
+        double s = 0.0;
+        for (int q = 0; q < kWppWarps; ++q)
+            s += reinterpret_cast<const double *>(smem + Ly.warp0 + q * Ly.per_warp + Ly.acc)[o];
+        w.partial[(size_t)blockIdx.x * 2 * nout + o] = s;
+    }
+}
+
+template <int S>
+int wpp_s_bytes(int nn, int nmat) { return (int)wpp_layout(nn, nmat, S).bytes; }
+
+template <int S, bool PHILOX>
+cudaError_t wpp_launch_s(const DevModel &m, const float *z, uint64_t seed, int64_t path0, const Work &w,
+                         cudaStream_t st)
+{
+    const int bytes = wpp_s_bytes<S>(m.nn, m.nmat);
+    cudaError_t e = cudaFuncSetAttribute(k_wpp<S, PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    k_wpp<S, PHILOX><<<(unsigned)((int64_t)m.nscen * w.items), kWppBlock, bytes, st>>>(m, z, seed, path0, w);
+    return cudaGetLastError();
+}
+
+template <int S, bool PHILOX>
+cudaError_t wpp_occ_s(int nn, int nmat, int *blocks)
+{
+    const int bytes = wpp_s_bytes<S>(nn, nmat);
+    cudaError_t e = cudaFuncSetAttribute(k_wpp<S, PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_wpp<S, PHILOX>, kWppBlock, bytes);
+}
+
+// Slots per lane for a shape: the smallest instantiated S with 32*S >= nn.
+int wpp_slots(int nn)
+{
+    if (nn <= 64) return 2;
+    if (nn <= 96) return 3;
+    if (nn <= 160) return 5;
+    if (nn <= 256) return 8;
+    return 0;
+}
+
+}  // namespace
+
+bool f32_wpp_supports(int nn, int nmat)
+{
+    return nn >= 2 && nn <= kMaxNN && nmat >= 1 && nmat < nn && wpp_slots(nn) > 0 &&
+           wpp_layout(nn, nmat, wpp_slots(nn)).bytes <= 227 * 1024;
+}
+
+int wpp_block_threads() { return kWppBlock; }
+
+cudaError_t wpp_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks)
 {
     *blocks = 0;
+    if (mode != Mode::Fused || !f32_wpp_supports(nn, nmat)) return cudaErrorNotSupported;
+    switch (wpp_slots(nn)) {
+        case 2: return philox ? wpp_occ_s<2, true>(nn, nmat, blocks) : wpp_occ_s<2, false>(nn, nmat, blocks);
+        case 3: return philox ? wpp_occ_s<3, true>(nn, nmat, blocks) : wpp_occ_s<3, false>(nn, nmat, blocks);
+        case 5: return philox ? wpp_occ_s<5, true>(nn, nmat, blocks) : wpp_occ_s<5, false>(nn, nmat, blocks);
+        case 8: return philox ? wpp_occ_s<8, true>(nn, nmat, blocks) : wpp_occ_s<8, false>(nn, nmat, blocks);
+    }
     return cudaErrorNotSupported;
 }
-cudaError_t launch_wpp_any(const DevModel &, Mode, const float *, uint64_t, int64_t, bool,
-                           const Work &, float *, const double *, cudaStream_t)
+
+cudaError_t launch_wpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
+                           int64_t path0, bool philox, const Work &w, float *, const double *,
+                           cudaStream_t s)
 {
+    if (mode != Mode::Fused || !f32_wpp_supports(m.nn, m.nmat)) return cudaErrorNotSupported;
+    switch (wpp_slots(m.nn)) {
+        case 2: return philox ? wpp_launch_s<2, true>(m, z, seed, path0, w, s) : wpp_launch_s<2, false>(m, z, seed, path0, w, s);
+        case 3: return philox ? wpp_launch_s<3, true>(m, z, seed, path0, w, s) : wpp_launch_s<3, false>(m, z, seed, path0, w, s);
+        case 5: return philox ? wpp_launch_s<5, true>(m, z, seed, path0, w, s) : wpp_launch_s<5, false>(m, z, seed, path0, w, s);
+        case 8: return philox ? wpp_launch_s<8, true>(m, z, seed, path0, w, s) : wpp_launch_s<8, false>(m, z, seed, path0, w, s);
+    }
     return cudaErrorNotSupported;
 }
 

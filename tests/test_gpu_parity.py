@@ -245,3 +245,49 @@ def test_full_size_fp32_vs_fp64_on_gpu(P):
     assert_f32_close(g, r, cfg.nn, "4,194,304 paths")
     # rounding error far below the Monte Carlo error
     assert np.all(np.abs(g - r) <= 0.05 * se + 1e-12)
+
+
+def _random_cfg(nn, nmat, nopt, seed, paths):
+    rng = np.random.default_rng(seed)
+    c = cfgs().LmmConfig(f"random{nn}x{nmat}", nn, nmat, 0.25, rng.uniform(0.02, 0.07, nn),
+                         rng.uniform(0.1, 0.3, nn), rng.integers(1, nn - nmat + 1, nopt).astype(np.int32),
+                         rng.uniform(0.03, 0.06, nopt), paths)
+    return c
+
+
+@pytest.mark.parametrize("philox", [False, True])
+def test_long_tenor_checkpointed_fp32_matches_oracle(P, philox):
+    """Workload 3 (NN=160, NMAT=120, 30 swaptions): warp-per-path kernel with the
+    reverse sweep recomputed from checkpoints every 8 steps."""
+    cfg = cfgs().workload(3, 512)
+    seed = 303
+    z = O.normals_f32(seed, cfg.paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        g, _ = e.greeks_philox(seed, cfg.paths) if philox else e.greeks_f32(z)
+    m, _ = O.greeks(cfg, z.astype(np.float64))
+    assert_f32_close(g[0], m, cfg.nn, f"160x120 philox={philox}")
+
+
+@pytest.mark.parametrize("nn,nmat,nopt", [(20, 10, 4), (33, 7, 3), (64, 32, 15), (96, 60, 8), (200, 150, 12)])
+def test_other_shapes_fp32_match_oracle(P, nn, nmat, nopt):
+    cfg = _random_cfg(nn, nmat, nopt, nn * 1000 + nmat, 700)
+    z = O.normals_f32(nn, cfg.paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        g, _ = e.greeks_f32(z)
+        g64, _ = e.greeks_f64(z.astype(np.float64))
+    m, _ = O.greeks(cfg, z.astype(np.float64))
+    np.testing.assert_allclose(g64[0], m, rtol=1e-11, atol=1e-12 * np.abs(m).max())
+    assert_f32_close(g[0], m, cfg.nn, f"{nn}x{nmat}")
+
+
+def test_pair_api_limited_to_reference_shape(P):
+    import torch
+    cfg = cfgs().workload(3, 64)
+    dz = torch.zeros(64 * cfg.nmat, dtype=torch.float32, device="cuda")
+    val = torch.zeros(1, dtype=torch.float64, device="cuda")
+    with P.Engine(cfg) as e:
+        t = e.tape(64)
+        with pytest.raises(P.LmmError) as ei:
+            e.forward_f32_device(dz.data_ptr(), 64, t, val.data_ptr())
+        assert ei.value.code == -2
+        t.close()
