@@ -25,9 +25,12 @@
 //   S += lambda_k Pb_i,   Pb_i += delta^2 lambda_k t r S     (S is the reference's v1)
 // and the vega of cell (n,i), k = i-n-1, is
 //   dV/dlambda_k += Pb_i (V_i + sqez - delta lambda_k) + delta^2 t S.
+// The kernel carries S' = delta^2 S (S' += delta^2 lambda_k Pb_i, Pb_i +=
+// lambda_k r t S'), which saves a multiply per cell. Vega slots of no-op cells
+// (k < 0) are NMAT spare rows per thread that are never read.
 // The reconstruction is a serial chain (exp -> rcp -> drift sum) per step, so
-// steps are processed in skewed pairs: cell (n,i) next to cell (n-1,i+1),
-// two independent chains in one instruction stream.
+// steps are processed as a skewed wavefront: cell (n,i) next to cell
+// (n-1,i+1) (and (n-2,i+2), ...), independent chains in one instruction stream.
 //
 // Cross-path reduction: per warp, each lane sums one output column over the
 // warp's 32 paths (shared-memory transpose), then adds into per-warp FP64
@@ -47,6 +50,17 @@
 #ifndef LMM_TPP_SEGR
 #define LMM_TPP_SEGR 4
 #endif
+// Reverse steps processed together as a skewed wavefront (independent
+// reconstruction chains per instruction stream): 2 or 4.
+#ifndef LMM_TPP_SKEW
+#define LMM_TPP_SKEW 2
+#endif
+// 1: arrange the reverse cell so that only FFMA -> ex2 -> FFMA -> rcp -> FFMA
+// sits on the reconstruction chain (three more instructions per cell).
+#ifndef LMM_TPP_SHORT
+#define LMM_TPP_SHORT 0
+#endif
+
 
 namespace lmm {
 namespace {
@@ -64,8 +78,8 @@ struct TppLayout {
     static constexpr int PAD = NMAT;                 // k = i-n-1 >= -NMAT
     static constexpr int NOUT = MODE == Mode::Fused ? 1 + 2 * NN : (MODE == Mode::Forward ? 1 : 2 * NN);
     static constexpr int kc = 0;                                     // float4[PAD+NN]
-    static constexpr int kx = kc + 16 * (PAD + NN);                  // float2[PAD+NN]
-    static constexpr int l0 = kx + 8 * (PAD + NN);                   // float[NN]
+    static constexpr int kx = kc + 16 * (PAD + NN);                  // float[PAD+NN]
+    static constexpr int l0 = align16(kx + 4 * (PAD + NN));          // float[NN]
     static constexpr int il0 = l0 + 4 * NN;                          // float[NN]
     static constexpr int ost = il0 + 4 * NN;                         // int[M+1]
     static constexpr int okf = align16(ost + 4 * (M + 1));           // float[kMaxNopt]
@@ -118,9 +132,9 @@ __device__ __forceinline__ float fwd_step(float (&L)[NN], const float4 *kcn, flo
 }
 
 struct RevStep {
-    float V, S, sqez;
+    float V, S, sqez;   // S holds delta^2 times the reference's v1
     const float4 *kc;   // kc[i]: constants of k = i-n-1
-    const float2 *kx;   // kx[i]: {delta*lambda_k, 1}, zero for k < 0
+    const float *kx;    // kx[i]: delta*lambda_k, zero for k < 0
     float *vg;          // vg[i*B]: this thread's vega slot of k = i-n-1
 };
 
@@ -130,43 +144,55 @@ __device__ __forceinline__ void rev_cell(float (&L)[NN], float (&Pb)[NN], RevSte
                                          float delta, float d2)
 {
     const float4 k = s.kc[i];
-    const float2 x = s.kx[i];
+    const float dlk = s.kx[i];
     const float y = s.V + s.sqez;
+#if LMM_TPP_SHORT
+    const float lp = L[i];
+    const float E = ex2_approx(-fmaf(k.x, s.V, fmaf(k.x, s.sqez, k.y)));
+    const float Ln = lp * E;
+    const float r = rcp_approx(fmaf(delta * lp, E, 1.0f));
+    const float t = Ln * r;
+    s.V = fmaf(-(k.z * Ln), r, s.V);
+#else
     const float Ln = L[i] * ex2_approx(-fmaf(k.x, y, k.y));
     const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
     const float t = Ln * r;
     s.V = fmaf(-k.z, t, s.V);
+#endif
     const float pb = Pb[i];
-    s.S = fmaf(k.w, pb, s.S);
+    s.S = fmaf(k.z, pb, s.S);
     const float tS = t * s.S;
     float *v = s.vg + i * B;
-    *v += x.y * fmaf(pb, y - x.x, d2 * tS);
-    Pb[i] = fmaf(k.z * r, tS, pb);
+    *v += fmaf(pb, y - dlk, tS);
+    Pb[i] = fmaf(k.w * r, tS, pb);
     L[i] = Ln;
 }
 
-// Steps hi = n and lo = n-1 together, skewed by one rate: at position i the
-// cells (hi, i) and (lo, i+1) are independent.
-template <int NN, int B, int I0>
-__device__ __forceinline__ void rev_pair(float (&L)[NN], float (&Pb)[NN], RevStep &hi, RevStep &lo,
-                                         float delta, float d2)
+// Steps n, n-1, ..., n-G+1 together, step n-g skewed by g rates: at position
+// i the cells (n-g, i+g) are independent of each other, and cell (n-g, i+g)
+// finds L_{n-g+1, i+g} written by cell (n-g+1, i+g) one position earlier.
+template <int NN, int B, int I0, int G>
+__device__ __forceinline__ void rev_group(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
+                                          float delta, float d2)
 {
 #pragma unroll
-    for (int i = NN - 1; i >= I0 - 1; --i) {
-        if (i >= I0) rev_cell<NN, B>(L, Pb, hi, i, delta, d2);
-        if (i + 1 <= NN - 1) rev_cell<NN, B>(L, Pb, lo, i + 1, delta, d2);
+    for (int i = NN - 1; i >= I0 - (G - 1); --i) {
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+            if (i + g >= I0 && i + g <= NN - 1) rev_cell<NN, B>(L, Pb, st[g], i + g, delta, d2);
     }
 }
 
 // Portfolio value, portfolio_b :133-171 and :186-197. Reciprocals are the
 // correctly rounded FP32 1/(1+delta L); the discount and annuity products,
 // the annuity sum and the payoffs are FP64. Returns the discounted value;
-// *disc_out, *b_out receive the discount factor and the last annuity factor,
-// *mask_out which swaptions (in grouped order) paid.
-template <int NN, int NMAT>
+// *disc_out receives the discount factor, *mask_out which swaptions (in
+// grouped order) paid, and Bst[m*B] (if given) the annuity factors B[m] of
+// :139 rounded to FP32, for the adjoint.
+template <int NN, int NMAT, int B>
 __device__ __forceinline__ double payoff_forward(const float (&L)[NN], float delta, const int *ost,
-                                                 const double *oKd, double *disc_out,
-                                                 double *b_out, unsigned long long *mask_out)
+                                                 const double *oKd, double *disc_out, float *Bst,
+                                                 unsigned long long *mask_out)
 {
     constexpr int M = NN - NMAT;
     double disc = 1.0;
@@ -179,6 +205,7 @@ __device__ __forceinline__ double payoff_forward(const float (&L)[NN], float del
     for (int m = 0; m < M; ++m) {
         b *= (double)__frcp_rn(fmaf(delta, L[NMAT + m], 1.0f));
         s = fma(dd, b, s);
+        if (Bst) Bst[m * B] = (float)b;
         const int o1 = ost[m + 1];
         for (int o = ost[m]; o < o1; ++o) {
             const double sw = fma(oKd[o], s, b) - 1.0;
@@ -189,29 +216,29 @@ __device__ __forceinline__ double payoff_forward(const float (&L)[NN], float del
         }
     }
     *disc_out = disc;
-    *b_out = b;
     *mask_out = mask;
     return disc * vs;
 }
 
 // Payoff adjoint, portfolio_b :173-184 (with the rate and its adjoint kept
 // apart) and :199-209, seeded with vbar = dOut/dV. Writes the log-adjoints
-// Pb[i] = L_i dOut/dL_i of the terminal rates.
-template <int NN, int NMAT>
+// Pb[i] = L_i dOut/dL_i of the terminal rates. Bst[m*B] holds B[m] from the
+// forward: rebuilding B[m-1] = B[m](1 + delta L) backwards from the last,
+// smallest factor would underflow FP32 on paths whose rates grow large.
+template <int NN, int NMAT, int B>
 __device__ __forceinline__ void payoff_adjoint(const float (&L)[NN], float (&Pb)[NN], float vbar,
-                                               double V, double disc, double bM,
+                                               double V, double disc, const float *Bst,
                                                unsigned long long mask, float delta,
                                                const int *ost, const float *oKf)
 {
     constexpr int M = NN - NMAT;
     const float scale = -vbar * (float)disc * delta;
-    float Bm = (float)bM;      // B[m] of :139, rebuilt backwards: B[m-1] = B[m] (1 + delta L)
     float Sb = 0.0f, Bb = 0.0f;
 #pragma unroll
     for (int m = M - 1; m >= 0; --m) {
         const float Ln = L[NMAT + m];
-        const float den = fmaf(delta, Ln, 1.0f);
-        const float r = __frcp_rn(den);
+        const float r = __frcp_rn(fmaf(delta, Ln, 1.0f));
+        const float Bm = Bst[m * B];
         const int o1 = ost[m + 1];
         for (int o = ost[m]; o < o1; ++o) {
             if ((mask >> o) & 1ull) {
@@ -222,7 +249,6 @@ __device__ __forceinline__ void payoff_adjoint(const float (&L)[NN], float (&Pb)
         Bb = fmaf(delta, Sb, Bb);
         Pb[NMAT + m] = scale * Bb * Bm * (Ln * r);
         Bb *= r;
-        Bm *= den;
     }
     const float vs = -vbar * (float)V * delta;
 #pragma unroll
@@ -284,39 +310,33 @@ __device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, f
 // Reverse over all steps, segments from the last, pairs (n, n-1) within each.
 template <int NN, int NMAT, int SEG, bool PHILOX, Mode MODE, int S = SEG - 1>
 __device__ __forceinline__ void reverse_all(float (&L)[NN], float (&Pb)[NN], const float4 *kc0,
-                                            const float2 *kx0, float *vg0, float4 &zq,
+                                            const float *kx0, float *vg0, float4 &zq,
                                             float4 &zq_next, const float *zp, uint64_t seed,
                                             uint64_t gpath, float sqd, float delta, float d2,
                                             const float *vt_s, const float *tape_v, int64_t total)
 {
     if constexpr (S >= 0) {
         constexpr int lo = S * NMAT / SEG, hi = (S + 1) * NMAT / SEG;
-        static_assert((hi - lo) % 2 == 0, "reverse segments hold whole step pairs");
+        constexpr int G = LMM_TPP_SKEW;
+        static_assert((hi - lo) % G == 0 && (G == 2 || G == 4), "reverse segments hold whole step groups");
         constexpr int B = kTppBlock;
-        for (int n = hi - 1; n > lo; n -= 2) {
+        for (int n = hi - 1; n > lo; n -= G) {
             if ((n & 3) == 3) {
                 zq = zq_next;
                 if ((n >> 2) > 0) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) - 1);
             }
-            RevStep h, l;
-            h.sqez = sqd * pick4(zq, n & 3);
-            l.sqez = sqd * pick4(zq, (n - 1) & 3);
-            if (MODE == Mode::Fused) {
-                h.V = vt_s[n * B];
-                l.V = vt_s[(n - 1) * B];
-            } else {
-                h.V = tape_v[(int64_t)n * total];
-                l.V = tape_v[(int64_t)(n - 1) * total];
+            RevStep st[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const int m = n - g;
+                st[g].sqez = sqd * pick4(zq, m & 3);
+                st[g].V = MODE == Mode::Fused ? vt_s[m * B] : tape_v[(int64_t)m * total];
+                st[g].S = 0.0f;
+                st[g].kc = kc0 - (m + 1);
+                st[g].kx = kx0 - (m + 1);
+                st[g].vg = vg0 - (m + 1) * B;
             }
-            h.S = 0.0f;
-            l.S = 0.0f;
-            h.kc = kc0 - (n + 1);
-            l.kc = kc0 - n;
-            h.kx = kx0 - (n + 1);
-            l.kx = kx0 - n;
-            h.vg = vg0 - (n + 1) * B;
-            l.vg = vg0 - n * B;
-            rev_pair<NN, B, lo + 1>(L, Pb, h, l, delta, d2);
+            rev_group<NN, B, lo + 1, G>(L, Pb, st, delta, d2);
         }
         reverse_all<NN, NMAT, SEG, PHILOX, MODE, S - 1>(L, Pb, kc0, kx0, vg0, zq, zq_next, zp, seed,
                                                         gpath, sqd, delta, d2, vt_s, tape_v, total);
@@ -333,7 +353,7 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     static_assert(NMAT % 4 == 0, "normals are read in aligned quads");
     extern __shared__ __align__(16) unsigned char smem[];
     float4 *kc_s = reinterpret_cast<float4 *>(smem + Lay::kc);
-    float2 *kx_s = reinterpret_cast<float2 *>(smem + Lay::kx);
+    float *kx_s = reinterpret_cast<float *>(smem + Lay::kx);
     float *l0_s = reinterpret_cast<float *>(smem + Lay::l0);
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
@@ -348,7 +368,7 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     for (int i = tid; i < PAD + NN; i += B) {
         const int k = i - PAD;
         kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
-        kx_s[i] = k < 0 ? make_float2(0.f, 0.f) : make_float2(m.kd[k], 1.0f);
+        kx_s[i] = k < 0 ? 0.0f : m.kd[k];
     }
     for (int i = tid; i < NN; i += B) {
         l0_s[i] = m.L0f[scen * NN + i];
@@ -368,7 +388,7 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     const int64_t ibase = (int64_t)item * w.ppt * B;
     const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
     const float4 *kc0 = kc_s + PAD;
-    const float2 *kx0 = kx_s + PAD;
+    const float *kx0 = kx_s + PAD;
     float *vg0 = vg_s + PAD * B + tid;
     float *vt0 = vt_s + tid;
 
@@ -401,12 +421,14 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             for (int i = 0; i < NN; ++i) L[i] = tape[(int64_t)i * total + tp];
         }
 
-        double disc = 1.0, bM = 1.0;
+        double disc = 1.0;
         unsigned long long mask = 0ull;
-        const double V = payoff_forward<NN, NMAT>(L, delta, ost_s, okd_s, &disc, &bM, &mask);
+        // B[m] goes to this thread's vega column, unused until the reverse sweep.
+        float *Bst = MODE == Mode::Forward ? nullptr : vg0;
+        const double V = payoff_forward<NN, NMAT, B>(L, delta, ost_s, okd_s, &disc, Bst, &mask);
 
         if (MODE != Mode::Forward) {
-            payoff_adjoint<NN, NMAT>(L, Pb, vb, V, disc, bM, mask, delta, ost_s, okf_s);
+            payoff_adjoint<NN, NMAT, B>(L, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s);
 #pragma unroll
             for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
             zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);

@@ -10,10 +10,10 @@
 //     is the mirror image (local suffix + exclusive warp suffix scan).
 // The forward stores the rates every kWppCkpt steps in shared memory. The
 // reverse sweep restores each checkpoint, recomputes its kWppCkpt steps
-// keeping t = L/(1+delta L) and the drift sums of every cell in registers,
+// keeping the pre-step rates and the drift sums of every cell in registers,
 // then runs the adjoint of those steps backwards (Pb = L dV/dL, the
 // log-adjoint):
-//   S_i = sum_{j>=i} lambda_k Pb_j,  Pb_i += delta^2 lambda_k t r S_i,  r = 1 - delta t
+//   S_i = sum_{j>=i} lambda_k Pb_j,  Pb_i += delta^2 lambda_k t r S_i
 //   dV/dlambda_k += Pb_i (V_i + sqez - delta lambda_k) + delta^2 t S_i.
 // The payoff (portfolio_b :120-211, aliasing fixed) runs with FP64 products:
 // the discount product is a warp product reduction, the annuity recursion
@@ -32,7 +32,7 @@ __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(
 // Shared-memory layout (bytes), shared by host and device.
 struct WppLay {
     int nn, nmat, S, nck, nout, M;
-    size_t kc, kd, l0, il0, ost, okf, okd, warp0, per_warp, ck, vg, lw, acc, bytes;
+    size_t kc, kd, l0, il0, ost, okf, okd, warp0, per_warp, ck, vg, lw, bw, acc, bytes;
 };
 
 __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
@@ -57,12 +57,16 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
     L.ck = w; w = al16(w + 4 * (size_t)L.nck * 32 * S);   // checkpoints [nck][32*S]
     L.vg = w; w = al16(w + 4 * (size_t)32 * S);           // vegas [32*S] (index k)
     L.lw = w; w = al16(w + 4 * (size_t)32 * S);           // payoff staging [32*S]
+    L.bw = w; w = al16(w + 4 * (size_t)32 * S);           // annuity factors B[m] [32*S]
     L.acc = w; w = al16(w + 8 * (size_t)2 * L.nout);      // FP64 sums [2*nout]
     L.per_warp = w;
     L.bytes = o + kWppWarps * w;
     return L;
 }
 
+// Exclusive warp scans. The exclusive value is the neighbour's inclusive
+// value (one more shuffle), not inclusive - x: that subtraction cancels
+// catastrophically when the lane's own term dominates the sum.
 __device__ __forceinline__ float warp_excl_prefix(float x, int lane)
 {
     float inc = x;
@@ -71,7 +75,8 @@ __device__ __forceinline__ float warp_excl_prefix(float x, int lane)
         const float y = __shfl_up_sync(0xffffffffu, inc, d);
         if (lane >= d) inc += y;
     }
-    return inc - x;
+    const float ex = __shfl_up_sync(0xffffffffu, inc, 1);
+    return lane == 0 ? 0.0f : ex;
 }
 
 __device__ __forceinline__ float warp_excl_suffix(float x, int lane)
@@ -82,16 +87,20 @@ __device__ __forceinline__ float warp_excl_suffix(float x, int lane)
         const float y = __shfl_down_sync(0xffffffffu, inc, d);
         if (lane + d < 32) inc += y;
     }
-    return inc - x;
+    const float ex = __shfl_down_sync(0xffffffffu, inc, 1);
+    return lane == 31 ? 0.0f : ex;
 }
 
-// One forward step n over the lane's slots. If T/Vs are given, the cell's t
-// and inclusive drift sum are kept (for the recompute of a checkpoint segment).
+// One forward step n over the lane's slots. If T/Vs are given, the cell's
+// pre-step rate and inclusive drift sum are kept (for the recompute of a
+// checkpoint segment). The rate, not t = L/(1+delta L), is kept: forming
+// r = 1/(1+delta L) again as 1 - delta t would cancel catastrophically on
+// paths whose rates grow large.
 template <int S>
 __device__ __forceinline__ void wpp_fwd_step(float (&L)[S], int n, float sqez, int lane, int nn,
                                              const float4 *kc, float delta, float (*T), float (*Vs))
 {
-    float a[S], t[S];
+    float a[S], Lpre[S];
     float4 kk[S];
     float P = 0.0f;
 #pragma unroll
@@ -100,8 +109,8 @@ __device__ __forceinline__ void wpp_fwd_step(float (&L)[S], int n, float sqez, i
         const bool act = i > n && i < nn;
         kk[s] = kc[act ? i - n - 1 : 0];
         const float r = rcp_approx(fmaf(delta, L[s], 1.0f));
-        t[s] = L[s] * r;
-        a[s] = act ? kk[s].z * t[s] : 0.0f;
+        Lpre[s] = L[s];
+        a[s] = act ? kk[s].z * (L[s] * r) : 0.0f;
         P += a[s];
         a[s] = P;                                   // local inclusive prefix
     }
@@ -113,7 +122,7 @@ __device__ __forceinline__ void wpp_fwd_step(float (&L)[S], int n, float sqez, i
         const float V = X + a[s];
         if (act) L[s] *= ex2_approx(fmaf(kk[s].x, V + sqez, kk[s].y));
         if (T) {
-            T[s] = t[s];
+            T[s] = Lpre[s];
             Vs[s] = V;
         }
     }
@@ -143,13 +152,16 @@ __device__ __forceinline__ void wpp_rev_step(float (&Pb)[S], int n, float sqez, 
             const int k = i - n - 1;
             const float4 kk = kc[k];
             const float Ssum = Y + b[s];
-            const float t = T[s];
-            const float r = fmaf(-delta, t, 1.0f);
+            const float r = rcp_approx(fmaf(delta, T[s], 1.0f));
+            const float t = T[s] * r;
             const float tS = t * Ssum;
             vg[k] += fmaf(Pb[s], Vs[s] + sqez - kd[k], d2 * tS);
             Pb[s] = fmaf(kk.z * r, tS, Pb[s]);
         }
     }
+    // The next step's vega slots overlap neighbouring lanes' slots of this
+    // step: order the shared-memory read-modify-writes across the warp.
+    __syncwarp();
 }
 
 template <bool PHILOX>
@@ -206,6 +218,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     float *ck_s = reinterpret_cast<float *>(wbase + Ly.ck);
     float *vg_s = reinterpret_cast<float *>(wbase + Ly.vg);
     float *lw_s = reinterpret_cast<float *>(wbase + Ly.lw);
+    float *bw_s = reinterpret_cast<float *>(wbase + Ly.bw);
     double *acc = reinterpret_cast<double *>(wbase + Ly.acc);
 
     const int scen = blockIdx.x / w.items, item = blockIdx.x % w.items;
@@ -267,6 +280,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             for (int mm = 0; mm < M; ++mm) {
                 bb *= (double)__frcp_rn(fmaf(delta, lw_s[nmat + mm], 1.0f));
                 ss = fma((double)delta, bb, ss);
+                bw_s[mm] = (float)bb;
                 for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
                     const double sw = fma(okd_s[o], ss, bb) - 1.0;
                     if (sw < 0.0) {
@@ -277,13 +291,15 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             }
             V = disc * vs;
             // :173-184 with the rate kept apart from its adjoint; lw_s[i] becomes
-            // the log-adjoint of rate i >= nmat.
+            // the log-adjoint of rate i >= nmat. B[m] comes from the forward
+            // (bw_s): rebuilding it backwards from the last, smallest factor
+            // would underflow FP32 on paths whose rates grow large.
             const float scale = -(float)disc * delta;
-            float Bm = (float)bb, Sb = 0.0f, Bb = 0.0f;
+            float Sb = 0.0f, Bb = 0.0f;
             for (int mm = M - 1; mm >= 0; --mm) {
                 const float Ln = lw_s[nmat + mm];
-                const float den = fmaf(delta, Ln, 1.0f);
-                const float r = __frcp_rn(den);
+                const float r = __frcp_rn(fmaf(delta, Ln, 1.0f));
+                const float Bm = bw_s[mm];
                 for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
                     if ((mask >> o) & 1ull) {
                         Sb -= 100.0f * okf_s[o];
@@ -293,7 +309,6 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 Bb = fmaf(delta, Sb, Bb);
                 lw_s[nmat + mm] = scale * Bb * Bm * (Ln * r);
                 Bb *= r;
-                Bm *= den;
             }
         }
         V = __shfl_sync(0xffffffffu, V, 0);
