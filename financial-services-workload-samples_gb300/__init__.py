@@ -32,7 +32,7 @@ EXPORTS = (
     "lmm_tape_create", "lmm_tape_destroy", "lmm_forward_f32_device", "lmm_backward_f32_device",
     "lmm_greeks_f64_host", "lmm_greeks_f64_device", "lmm_bump_greeks_f64_device",
     "lmm_bump_greeks_f64_host", "lmm_normals_f32_device", "lmm_normals_f64_device",
-    "lmm_swaption_greeks", "lmm_swaption_greeks_f32",
+    "lmm_swaption_greeks", "lmm_swaption_greeks_f32", "lmm_greeks_f32_device_noalloc",
 )
 
 
@@ -98,6 +98,7 @@ def lib():
         "lmm_normals_f64_device": ([u64, i64, i64, i32, C.c_double, C.c_double, vp, vp], C.c_int),
         "lmm_swaption_greeks": ([dp, C.c_int, C.c_double, C.c_double, C.c_int, dp, dp, C.c_int], C.c_int),
         "lmm_swaption_greeks_f32": ([fp, C.c_int, C.c_float, C.c_float, C.c_int, fp, fp, C.c_int], C.c_int),
+        "lmm_greeks_f32_device_noalloc": ([P, vp, i64, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -1,0 +1,177 @@
+// lmm_greeks_f32_device_noalloc: the fused FP32 value + Greeks launch for
+// callers that cannot allocate device memory.
+//
+// Some callers cannot call cudaMalloc: code embedded in a host application
+// that owns every device allocation through its own pool, a plug-in whose
+// process has exhausted or locked its allocator, or a latency-critical loop
+// that must not touch the allocator at all. This entry point needs no engine
+// and allocates nothing. Its scratch -- the model constants, the per-block
+// FP64 partial sums and the non-finite flag -- lives in one file-scope static
+// device array of kScratchBytes, which every GPU that loads the library holds
+// until the process exits.
+//
+// Host code must not pass g_noalloc_scratch itself to a kernel: in host code
+// that name is a host-side stand-in, not a device address. The first call on
+// each device (with that device current) looks the address up with
+// cudaGetSymbolAddress, queries the kernel's occupancy and caches both; make
+// that first call before any stream capture.
+#include "lmm_gb300.h"
+#include "lmm_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <mutex>
+
+namespace {
+
+constexpr int kNN = 80, kNMAT = 40, kM = kNN - kNMAT, kNout = 1 + 2 * kNN;
+constexpr size_t kScratchBytes = LMM_NOALLOC_SCRATCH_BYTES;
+constexpr int kMaxDevices = 64;
+
+// Model section of the scratch, uploaded by every call (device layout).
+struct NoallocModel {
+    float4 kc[kNN];
+    float kd[kNN];
+    float L0f[LMM_NOALLOC_MAX_SCEN * kNN];
+    float iL0f[LMM_NOALLOC_MAX_SCEN * kNN];
+    double L0d[LMM_NOALLOC_MAX_SCEN * kNN];
+    double lamd[kNN];
+    int ost[kM + 1];
+    float okf[LMM_MAX_NOPT];
+    double okd[LMM_MAX_NOPT];
+};
+
+constexpr size_t kModelBytes = (sizeof(NoallocModel) + 255) & ~size_t(255);
+constexpr size_t kFlagBytes = 256;
+constexpr size_t kPartialBytes = kScratchBytes - kModelBytes - kFlagBytes;
+constexpr int kMaxItems = (int)(kPartialBytes / (sizeof(double) * 2 * kNout));
+static_assert(kMaxItems >= 64 * LMM_NOALLOC_MAX_SCEN, "scratch too small");
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+struct DeviceSetup {
+    bool ready = false;
+    unsigned char *scratch = nullptr;   // device address of g_noalloc_scratch
+    int sms = 0, bps = 0;
+};
+
+std::mutex g_mu;
+DeviceSetup g_setup[kMaxDevices];
+
+int setup_device(int dev, DeviceSetup *out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    DeviceSetup &s = g_setup[dev];
+    if (!s.ready) {
+        void *ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return LMM_ERR_CUDA;
+        int sms = 0, bps = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return LMM_ERR_CUDA;
+        if (lmm::tpp_blocks_per_sm(lmm::Mode::Fused, false, &bps) != cudaSuccess || bps < 1) return LMM_ERR_CUDA;
+        s.scratch = static_cast<unsigned char *>(ptr);
+        s.sms = sms;
+        s.bps = bps;
+        s.ready = true;
+    }
+    *out = s;
+    return LMM_OK;
+}
+
+}  // namespace
+
+extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d_z, int64_t paths,
+                                             double *d_out, double *d_se, void *stream)
+{
+    int rc = lmm_validate_params(p);
+    if (rc != LMM_OK) return rc;
+    if (p->nn != kNN || p->nmat != kNMAT) return LMM_ERR_UNSUPPORTED;
+    if (p->nscen > LMM_NOALLOC_MAX_SCEN) return LMM_ERR_TOO_LARGE;
+    if (!d_z || !d_out || paths < 1) return LMM_ERR_INVALID_ARG;
+    if (paths > (int64_t(1) << 40)) return LMM_ERR_TOO_LARGE;
+
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return LMM_ERR_NO_DEVICE;
+    if (dev < 0 || dev >= kMaxDevices) return LMM_ERR_UNSUPPORTED;
+    DeviceSetup ds;
+    if ((rc = setup_device(dev, &ds)) != LMM_OK) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    // Model constants, built on the host stack in the device layout.
+    NoallocModel hm;
+    std::memset(&hm, 0, sizeof(hm));
+    const double d = p->delta, log2e = 1.4426950408889634073599246810019;
+    for (int k = 0; k < kNN; ++k) {
+        const double l = p->lambda[k];
+        hm.kc[k] = make_float4((float)(l * log2e), (float)(-0.5 * d * l * l * log2e), (float)(d * d * l), (float)l);
+        hm.kd[k] = (float)(d * l);
+        hm.lamd[k] = l;
+    }
+    for (int i = 0; i < p->nscen * kNN; ++i) {
+        hm.L0f[i] = (float)p->L0[i];
+        hm.iL0f[i] = 1.0f / hm.L0f[i];
+        hm.L0d[i] = p->L0[i];
+    }
+    // options grouped by swap length (a counting sort keeps the input order)
+    int cnt[kM + 2] = {0};
+    for (int o = 0; o < p->nopt; ++o) cnt[p->maturities[o]] += 1;
+    for (int m = 0; m <= kM; ++m) hm.ost[m] = (m == 0 ? 0 : hm.ost[m - 1] + cnt[m]);
+    int fill[kM + 1];
+    for (int m = 0; m <= kM; ++m) fill[m] = hm.ost[m];
+    for (int o = 0; o < p->nopt; ++o) {
+        const int slot = fill[p->maturities[o] - 1]++;
+        hm.okf[slot] = (float)p->swaprates[o];
+        hm.okd[slot] = p->swaprates[o];
+    }
+
+    unsigned char *base = ds.scratch;
+    if (cudaMemcpyAsync(base, &hm, sizeof(hm), cudaMemcpyHostToDevice, st) != cudaSuccess) return LMM_ERR_CUDA;
+    const NoallocModel *dmod = reinterpret_cast<const NoallocModel *>(base);
+    int *flag = reinterpret_cast<int *>(base + kModelBytes);
+    double *partial = reinterpret_cast<double *>(base + kModelBytes + kFlagBytes);
+
+    lmm::DevModel m{};
+    m.nn = kNN;
+    m.nmat = kNMAT;
+    m.nopt = p->nopt;
+    m.nscen = p->nscen;
+    m.delta = (float)d;
+    m.sqd = (float)std::sqrt(d);
+    m.d2 = (float)(d * d);
+    m.deltad = d;
+    m.sqdd = std::sqrt(d);
+    m.kc = dmod->kc;
+    m.kd = dmod->kd;
+    m.L0f = dmod->L0f;
+    m.invL0f = dmod->iL0f;
+    m.L0d = dmod->L0d;
+    m.lamd = dmod->lamd;
+    m.opt_start = dmod->ost;
+    m.optKf = dmod->okf;
+    m.optKd = dmod->okd;
+
+    // About two waves of the device, capped by the partial-sum space.
+    const int64_t block = lmm::tpp_block_threads();
+    const int64_t nscen = p->nscen;
+    int64_t items = (2 * (int64_t)ds.sms * ds.bps + nscen - 1) / nscen;
+    if (items * nscen > kMaxItems) items = kMaxItems / nscen;
+    if (items < 1) items = 1;
+    int64_t ppt = (paths + block * items - 1) / (block * items);
+    items = (paths + block * ppt - 1) / (block * ppt);
+    if (ppt > 0x7fffffff) return LMM_ERR_TOO_LARGE;
+    lmm::Work w{};
+    w.paths = paths;
+    w.items = (int)items;
+    w.ppt = (int)ppt;
+    w.partial = partial;
+    w.nout = kNout;
+
+    if (cudaMemsetAsync(flag, 0, sizeof(int), st) != cudaSuccess) return LMM_ERR_CUDA;
+    if (lmm::launch_tpp_any(m, lmm::Mode::Fused, d_z, 0, 0, false, w, nullptr, nullptr, st) != cudaSuccess)
+        return LMM_ERR_CUDA;
+    if (lmm::launch_finalize(partial, p->nscen, w.items, kNout, paths, d_out, d_se, flag, st) != cudaSuccess)
+        return LMM_ERR_CUDA;
+    return LMM_OK;
+}

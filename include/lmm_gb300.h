@@ -163,6 +163,35 @@ int lmm_normals_f32_device(uint64_t seed, int64_t path0, int64_t paths, int32_t 
 int lmm_normals_f64_device(uint64_t seed, int64_t path0, int64_t paths, int32_t nmat,
                            double mean, double std_dev, double *d_z, void *stream);
 
+/* ---- no-allocation variant ---------------------------------------------- */
+/* No counterpart in the reference. Some callers cannot call cudaMalloc: a
+ * library embedded in a host application that owns every device allocation
+ * through its own pool, a plug-in whose process has locked or exhausted its
+ * allocator, a loop that must never touch the allocator. This is the fused
+ * FP32 value + Greeks launch of lmm_greeks_f32_device without an engine and
+ * without any allocation (no cudaMalloc, no cudaFree, no allocating library
+ * call). The caller passes the parameters, the device normals d_z and the
+ * device outputs d_out/d_se (layout as above); everything else -- model
+ * constants, per-block partial sums, the non-finite flag -- lives in one
+ * static device array of LMM_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * the library holds until the process exits.
+ *   - Limits: nn = 80, nmat = 40 (LMM_ERR_UNSUPPORTED otherwise),
+ *     nscen <= LMM_NOALLOC_MAX_SCEN and paths <= 2^40 (LMM_ERR_TOO_LARGE).
+ *   - Works on the current device and enqueues on `stream`. The model
+ *     constants are copied from host memory on the way in, so the call
+ *     returns only after earlier work on `stream` has drained.
+ *   - The first call on a device looks up the array's device address and the
+ *     kernel's occupancy and caches them: make it before any stream capture.
+ *   - Every call shares the one array, which keeps the last call's
+ *     contents: calls that overlap on the GPU (other streams, other host
+ *     threads) race on it and must be serialised by the caller.
+ *   - Non-finite results are not reported (there is no engine to hold the
+ *     flag); check d_out. lmm_last_error() is not updated. */
+#define LMM_NOALLOC_SCRATCH_BYTES (4u << 20)
+#define LMM_NOALLOC_MAX_SCEN 8
+int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d_z, int64_t paths,
+                                  double *d_out, double *d_se, void *stream);
+
 /* ---- the reference's signature ---------------------------------------- */
 /* Drop-in for liborSwaptionGreeks (liborSwaptionGreeks.hpp:12-13) in the
  * reference's FP64 build (REAL = double, params.h:10-16): fills z[0..num)

@@ -1,0 +1,77 @@
+"""The no-allocation entry point, lmm_greeks_f32_device_noalloc.
+
+It serves callers that cannot allocate device memory (a host application that
+owns every allocation through its own pool, a process whose allocator is
+locked): it runs the same fused FP32 kernel as lmm_greeks_f32_device, with its
+scratch in a static device array instead of an engine's buffers. This file is
+named to be collected last; it passes alone in a fresh process too.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import cfgs, pkg
+
+pytestmark = pytest.mark.gpu
+
+
+def _scaled_err(g, r, nn):
+    out = []
+    for sl in (slice(0, 1), slice(1, 1 + nn), slice(1 + nn, 1 + 2 * nn)):
+        floor = 1e-2 * np.abs(r[sl]).max() if r[sl].size > 1 else 0.0
+        den = np.maximum(np.abs(r[sl]), max(floor, 1e-300))
+        out.append(np.max(np.abs(g[sl] - r[sl]) / den))
+    return max(out)
+
+
+def _call(P, cfg, dz, paths, out, se, stream):
+    ref = P._ParamsRef(cfg)
+    return P.lib().lmm_greeks_f32_device_noalloc(C.byref(ref.p), dz.data_ptr(), paths, out.data_ptr(),
+                                                 se.data_ptr(), C.c_void_p(stream))
+
+
+@pytest.mark.parametrize("nscen", [1, 3])
+def test_noalloc_matches_engine_on_two_calls_in_a_row(nscen):
+    import torch
+    P = pkg()
+    base = cfgs().workload(5 if nscen > 1 else 4, 100_003)
+    cfg = base.with_paths(base.paths)
+    if nscen > 1:
+        cfg.L0 = base.L0[:nscen].copy()
+    n = cfg.paths
+    dz = torch.empty(n * cfg.nmat, dtype=torch.float32, device="cuda")
+    P.normals_f32_device(77, n, cfg.nmat, dz.data_ptr())
+    ref = torch.zeros(nscen * cfg.nout, dtype=torch.float64, device="cuda")
+    ref_se = torch.zeros_like(ref)
+    with P.Engine(cfg) as e:
+        e.greeks_f32_device(dz.data_ptr(), n, ref.data_ptr(), ref_se.data_ptr())
+        e.synchronize()
+    r = ref.cpu().numpy().reshape(nscen, cfg.nout)
+    r_se = ref_se.cpu().numpy().reshape(nscen, cfg.nout)
+    stream = torch.cuda.current_stream().cuda_stream
+    for call in range(2):
+        out = torch.full((nscen * cfg.nout,), np.nan, dtype=torch.float64, device="cuda")
+        se = torch.full_like(out, np.nan)
+        assert _call(P, cfg, dz, n, out, se, stream) == 0
+        torch.cuda.synchronize()
+        g = out.cpu().numpy().reshape(nscen, cfg.nout)
+        g_se = se.cpu().numpy().reshape(nscen, cfg.nout)
+        for s in range(nscen):
+            # same kernel and arithmetic; only the FP64 summation grouping may differ
+            assert _scaled_err(g[s], r[s], cfg.nn) <= 1e-4
+            np.testing.assert_allclose(g[s], r[s], rtol=1e-9, atol=1e-12 * np.abs(r[s]).max())
+            np.testing.assert_allclose(g_se[s], r_se[s], rtol=1e-6)
+
+
+def test_noalloc_limits_are_errors():
+    import torch
+    P = pkg()
+    dz = torch.zeros(64 * 120, dtype=torch.float32, device="cuda")
+    out = torch.zeros(321, dtype=torch.float64, device="cuda")
+    se = torch.zeros_like(out)
+    assert _call(P, cfgs().workload(3, 64), dz, 64, out, se, 0) == -2          # nn=160: unsupported
+    many = cfgs().workload(5, 64)                                              # 256 curves > 8
+    assert _call(P, many, dz, 64, out, se, 0) == -6
+    one = cfgs().workload(1, 64)
+    assert _call(P, one, dz, 0, out, se, 0) == -1
