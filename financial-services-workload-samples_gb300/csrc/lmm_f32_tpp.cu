@@ -48,12 +48,12 @@
 #define LMM_TPP_SEGF 8
 #endif
 #ifndef LMM_TPP_SEGR
-#define LMM_TPP_SEGR 4
+#define LMM_TPP_SEGR 5
 #endif
 // Reverse steps processed together as a skewed wavefront (independent
 // reconstruction chains per instruction stream): 2 or 4.
 #ifndef LMM_TPP_SKEW
-#define LMM_TPP_SKEW 2
+#define LMM_TPP_SKEW 4
 #endif
 // 1: arrange the reverse cell so that only FFMA -> ex2 -> FFMA -> rcp -> FFMA
 // sits on the reconstruction chain (three more instructions per cell).

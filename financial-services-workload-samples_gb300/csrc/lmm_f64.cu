@@ -24,8 +24,9 @@ struct F64Smem {
 };
 
 // portfolio_b :133-171 and :186-197 in FP64; returns the discounted value.
+// Bst (if given) receives the annuity factors B[m] of :139 for the adjoint.
 __device__ double payoff_value_f64(const double *L, int nn, int nmat, double d, const int *ost,
-                                   const double *okd, double *disc_out, double *b_out,
+                                   const double *okd, double *disc_out, double *Bst,
                                    unsigned long long *mask_out)
 {
     double b = 1.0, s = 0.0, vs = 0.0;
@@ -33,6 +34,7 @@ __device__ double payoff_value_f64(const double *L, int nn, int nmat, double d, 
     for (int m = 0; m < nn - nmat; ++m) {
         b = b / (1.0 + d * L[nmat + m]);
         s = s + d * b;
+        if (Bst) Bst[m] = b;
         for (int o = ost[m]; o < ost[m + 1]; ++o) {
             const double sw = b + okd[o] * s - 1.0;
             if (sw < 0.0) {
@@ -44,7 +46,6 @@ __device__ double payoff_value_f64(const double *L, int nn, int nmat, double d, 
     double disc = 1.0;
     for (int n = 0; n < nmat; ++n) disc = disc / (1.0 + d * L[n]);
     *disc_out = disc;
-    *b_out = b;
     *mask_out = mask;
     return disc * vs;
 }
@@ -86,7 +87,7 @@ k_f64_greeks(const DevModel m, const double *__restrict__ z, const Work w)
     const double d = m.deltad, sqd = m.sqdd;
     const double *L0 = m.L0d + (size_t)scen * nn;
 
-    double L[kMaxNN], Pb[kMaxNN], vg[kMaxNN], Vt[kMaxNN];
+    double L[kMaxNN], Pb[kMaxNN], vg[kMaxNN], Vt[kMaxNN], Bs[kMaxNN];
     const int64_t ibase = (int64_t)item * w.ppt * kF64Block;
     for (int j = 0; j < w.ppt; ++j) {
         if (ibase + (int64_t)j * kF64Block >= w.paths) break;
@@ -98,14 +99,17 @@ k_f64_greeks(const DevModel m, const double *__restrict__ z, const Work w)
             vg[i] = 0.0;
         }
         forward_f64(L, Vt, zp, lam_s, nn, nmat, d, sqd);
-        double disc, bM;
+        double disc;
         unsigned long long mask;
-        const double V = payoff_value_f64(L, nn, nmat, d, ost_s, okd_s, &disc, &bM, &mask);
+        const double V = payoff_value_f64(L, nn, nmat, d, ost_s, okd_s, &disc, Bs, &mask);
         // payoff adjoint (:173-184 with the rate kept apart from its adjoint,
-        // then :199-209), written as log-adjoints Pb = L * dV/dL.
+        // then :199-209), written as log-adjoints Pb = L * dV/dL. B[m] comes
+        // from the forward as in the reference: rebuilding it backwards from
+        // the last factor underflows on paths whose rates explode.
         {
-            double Bm = bM, Sb = 0.0, Bb = 0.0;
+            double Sb = 0.0, Bb = 0.0;
             for (int mm = M - 1; mm >= 0; --mm) {
+                const double Bm = Bs[mm];
                 const double Ln = L[nmat + mm];
                 for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
                     if ((mask >> o) & 1ull) {
@@ -117,7 +121,6 @@ k_f64_greeks(const DevModel m, const double *__restrict__ z, const Work w)
                 const double den = 1.0 + d * Ln;
                 Pb[nmat + mm] = disc * (-Bb * Bm * d / den) * Ln;
                 Bb = Bb / den;
-                Bm = Bm * den;
             }
             for (int n = 0; n < nmat; ++n) Pb[n] = (-V * d / (1.0 + d * L[n])) * L[n];
         }
@@ -195,9 +198,9 @@ k_f64_bump(const DevModel m, const double *__restrict__ z, double h, const Work 
         const double *zp = z + (active ? pl : w.paths - 1) * nmat;
         for (int i = 0; i < nn; ++i) L[i] = L0[i] + ((var >= 1 && var <= nn && i == var - 1) ? h : 0.0);
         forward_f64(L, nullptr, zp, lam_s, nn, nmat, d, sqd);
-        double disc, bM;
+        double disc;
         unsigned long long mask;
-        double V = payoff_value_f64(L, nn, nmat, d, ost_s, okd_s, &disc, &bM, &mask);
+        double V = payoff_value_f64(L, nn, nmat, d, ost_s, okd_s, &disc, nullptr, &mask);
         V = active ? V : 0.0;
         const double s1 = warp_sum(V), s2 = warp_sum(V * V);
         if (lane == 0) {
