@@ -64,6 +64,29 @@ def dist_env():
     return ws, rank, local
 
 
+def rank_path0(rank: int, paths_per_rank: int) -> int:
+    """First global path index of a rank: replicas take disjoint path ranges
+    (Philox counters are keyed by the global path index)."""
+    return rank * paths_per_rank
+
+
+def max_over_ranks(x: float, device=None) -> float:
+    """The slowest rank's time (any torch.distributed backend; identity when
+    not distributed)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: int, steps: int, world_size: int, t_max: float) -> float:
+    """Units processed by all ranks per second of the slowest rank."""
+    return world_size * units_per_rank * steps / t_max
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
 
@@ -187,7 +210,8 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
 
     dz = torch.empty(n * nmat, dtype=torch.float32, device=dev)
-    P.normals_f32_device(20260603, n, nmat, dz.data_ptr(), stream=stream.cuda_stream, path0=rank * n)
+    P.normals_f32_device(20260603, n, nmat, dz.data_ptr(), stream=stream.cuda_stream,
+                         path0=rank_path0(rank, n))
     out = torch.zeros(nout, dtype=torch.float64, device=dev)
     se = torch.zeros(nout, dtype=torch.float64, device=dev)
     eng = P.Engine(cfg, device=local)
@@ -223,12 +247,8 @@ def run_ours(args):
     res32 = out.cpu().numpy().copy()
     se32 = se.cpu().numpy().copy()
 
-    t_max = elapsed
-    if ws > 1:
-        t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = t.item()
-    value = ws * n * args.steps / t_max
+    t_max = max_over_ranks(elapsed, dev)
+    value = whole_job_rate(n, args.steps, ws, t_max)
 
     # ---- end to end through the host C-ABI call, pinned host normals -----
     hz = torch.empty(n * nmat, dtype=torch.float32, pin_memory=True)
@@ -240,12 +260,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         eng.greeks_f32(hz_np, n)
-    e2e_dt = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_dt], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_dt = t.item()
-    e2e = ws * n * args.steps / e2e_dt
+    e2e_dt = max_over_ranks(time.perf_counter() - t0, dev)
+    e2e = whole_job_rate(n, args.steps, ws, e2e_dt)
     e2e_launches = eng.last_launches
 
     # ---- accuracy: FP64 GPU kernel on the identical normals --------------
@@ -286,6 +302,31 @@ def run_ours(args):
                 "seconds": bt, "method": "FP64 forward re-run per bumped input (one-sided, h=1e-6)",
                 "fp32_adjoint_speedup": value / ws / (nb / bt)}
 
+    # ---- the other named workloads (one timed call each, after warm-up) ----
+    others = None
+    if rank == 0 and not args.skip_others:
+        others = {}
+        for wl, mode in ((3, "hbm"), (4, "philox"), (5, "hbm")):
+            c = P.configs.workload(wl)
+            with P.Engine(c, device=local) as ew:
+                ew.set_stream(stream.cuda_stream)
+                o = torch.zeros(c.nscen * c.nout, dtype=torch.float64, device=dev)
+                zw = None
+                if mode == "hbm":
+                    zw = torch.empty(c.paths * c.nmat, dtype=torch.float32, device=dev)
+                    P.normals_f32_device(wl, c.paths, c.nmat, zw.data_ptr(), stream=stream.cuda_stream)
+                run = (lambda: ew.greeks_f32_device(zw.data_ptr(), c.paths, o.data_ptr())) if mode == "hbm" \
+                    else (lambda: ew.greeks_philox_device(wl, c.paths, o.data_ptr()))
+                run()
+                ew.set_timing(True)
+                run()
+                kms = ew.kernel_time()[1]
+                others[c.name] = {"paths_per_s": c.nscen * c.paths / (kms * 1e-3), "ms": kms,
+                                  "nn": c.nn, "nmat": c.nmat, "scenarios": c.nscen, "normals": mode,
+                                  "kernel": "k_tpp (thread per path)" if c.nn == 80 else
+                                  "k_wpp (warp per path, checkpoints every 8 steps)"}
+                del zw
+
     # ---- roofline -----------------------------------------------------------
     roof = None
     if rank == 0:
@@ -318,7 +359,8 @@ def run_ours(args):
             "e2e": {"value": e2e, "unit": "paths/s", "h2d_bytes_per_step": 4 * n * nmat,
                     "d2h_bytes_per_step": 2 * 8 * nout + 4, "launches_per_step": e2e_launches,
                     "api": "lmm_greeks_f32_host (pinned host normals)"},
-            "roofline": roof, "clocks": clk.summary(), "accuracy": acc, "fp64_bump_comparator": bump}
+            "roofline": roof, "clocks": clk.summary(), "accuracy": acc, "fp64_bump_comparator": bump,
+            "other_workloads": others}
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline_port(cfg, target_s=args.cpu_seconds)
         line["cpu_baseline"].pop("seconds", None)
@@ -344,6 +386,7 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-bump", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-others", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

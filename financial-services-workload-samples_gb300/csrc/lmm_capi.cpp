@@ -101,6 +101,10 @@ struct lmm_engine {
     bool timing = false;
     bool timed = false;            // the last call recorded its events
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // begin, main kernel done, all done
+    // host-call pipelining: chunked host->device copies on their own stream
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_ev[8] = {};
+    cudaEvent_t ready_ev = nullptr;
 };
 
 struct lmm_tape {
@@ -204,6 +208,18 @@ int plan(lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int nout
     LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)(nvs * items) * 2 * nout));
     w->partial = e->partial.as<double>();
     return LMM_OK;
+}
+
+// Items/paths-per-thread of a launch without touching the scratch (see plan).
+void plan_items(const lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int64_t *items,
+                int64_t *ppt, int waves = 2)
+{
+    const int64_t cap = (int64_t)e->sms * bps;
+    const int64_t target = std::max<int64_t>(1, cap * waves);
+    int64_t it = std::max<int64_t>(1, (target + nvs - 1) / nvs);
+    int64_t p = std::max<int64_t>(1, (paths + block * it - 1) / (block * it));
+    *ppt = p;
+    *items = (paths + block * p - 1) / (block * p);
 }
 
 int check_paths(int64_t paths)
@@ -484,9 +500,16 @@ int lmm_engine_destroy(lmm_engine *e)
     e->se.release();
     e->flag.release();
     e->vbar.release();
+    if (e->copy_stream) {
+        cudaStreamSynchronize(e->copy_stream);
+        cudaStreamDestroy(e->copy_stream);
+    }
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
     for (auto &ev : e->ev)
         if (ev) cudaEventDestroy(ev);
+    for (auto &ev : e->copy_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (e->ready_ev) cudaEventDestroy(e->ready_ev);
     delete e;
     return LMM_OK;
 }
@@ -590,6 +613,74 @@ int lmm_greeks_f32_device(lmm_engine *e, const float *d_z, int64_t paths, double
     return run_f32(e, Mode::Fused, d_z, 0, 0, false, paths, nullptr, nullptr, d_out, d_se);
 }
 
+// Host call with the copy overlapped: the normals go up in kHostChunks
+// pieces on the engine's copy stream; the fused kernel of piece c starts as
+// soon as piece c has landed, while piece c+1 is still in flight. Each piece
+// writes its own range of partial sums and one ordered k_finalize covers them
+// all. Single-scenario engines only.
+constexpr int kHostChunks = 4;
+constexpr int64_t kPipelineMinPaths = int64_t(1) << 18;
+
+int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
+{
+    const int fam = f32_family(e);
+    if (fam == 0) return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for this shape");
+    int bps = 0;
+    LMM_TRY(blocks_per_sm(e, fam, Mode::Fused, false, &bps));
+    const int block = fam == 1 ? lmm::tpp_block_threads() : lmm::wpp_block_threads();
+    const int per_batch = fam == 1 ? block : block / 32;
+    const int nout = 1 + 2 * e->nn;
+    const int C = kHostChunks;
+    int64_t cpaths[kHostChunks], cfirst[kHostChunks], citems[kHostChunks], cppt[kHostChunks];
+    int64_t total_items = 0;
+    for (int c = 0; c < C; ++c) {
+        cfirst[c] = paths * c / C;
+        cpaths[c] = paths * (c + 1) / C - cfirst[c];
+        plan_items(e, 1, cpaths[c], per_batch, bps, &citems[c], &cppt[c]);
+        if (cppt[c] > INT32_MAX || citems[c] > INT32_MAX) return fail(LMM_ERR_TOO_LARGE, "launch too large");
+        total_items += citems[c];
+    }
+    LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)total_items * 2 * nout));
+    LMM_TRY(e->flag.ensure(sizeof(int)));
+    if (!e->copy_stream) LMM_CK(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));
+    if (!e->ready_ev) LMM_CK(cudaEventCreateWithFlags(&e->ready_ev, cudaEventDisableTiming));
+    for (int c = 0; c < C; ++c)
+        if (!e->copy_ev[c]) LMM_CK(cudaEventCreateWithFlags(&e->copy_ev[c], cudaEventDisableTiming));
+    // the copies must not overtake earlier work on the engine's stream
+    LMM_CK(cudaEventRecord(e->ready_ev, e->stream));
+    LMM_CK(cudaStreamWaitEvent(e->copy_stream, e->ready_ev, 0));
+    float *dz = e->z32.as<float>();
+    for (int c = 0; c < C; ++c) {
+        const size_t off = (size_t)cfirst[c] * e->nmat, n = (size_t)cpaths[c] * e->nmat;
+        LMM_CK(cudaMemcpyAsync(dz + off, z + off, sizeof(float) * n, cudaMemcpyHostToDevice, e->copy_stream));
+        LMM_CK(cudaEventRecord(e->copy_ev[c], e->copy_stream));
+    }
+    LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
+    mark(e, 0);
+    double *part = e->partial.as<double>();
+    for (int c = 0; c < C; ++c) {
+        LMM_CK(cudaStreamWaitEvent(e->stream, e->copy_ev[c], 0));
+        Work w{};
+        w.paths = cpaths[c];
+        w.items = (int)citems[c];
+        w.ppt = (int)cppt[c];
+        w.nout = nout;
+        w.partial = part;
+        const float *zc = dz + (size_t)cfirst[c] * e->nmat;
+        cudaError_t err = fam == 1
+                              ? lmm::launch_tpp_any(e->dm, Mode::Fused, zc, 0, 0, false, w, nullptr, nullptr, e->stream)
+                              : lmm::launch_wpp_any(e->dm, Mode::Fused, zc, 0, 0, false, w, nullptr, nullptr, e->stream);
+        if (err != cudaSuccess) return cuda_fail(err, "FP32 LMM kernel launch");
+        part += (size_t)citems[c] * 2 * nout;
+    }
+    mark(e, 1);
+    LMM_CK(lmm::launch_finalize(e->partial.as<double>(), 1, (int)total_items, nout, paths,
+                                e->out.as<double>(), e->se.as<double>(), e->flag.as<int>(), e->stream));
+    mark(e, 2);
+    e->last_launches = C + 1;
+    return LMM_OK;
+}
+
 int lmm_greeks_f32_host(lmm_engine *e, const float *z, int64_t paths, double *out, double *se)
 {
     if (!e || !z || !out) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
@@ -598,9 +689,13 @@ int lmm_greeks_f32_host(lmm_engine *e, const float *z, int64_t paths, double *ou
     const size_t zb = sizeof(float) * (size_t)paths * e->nmat;
     LMM_TRY(e->z32.ensure(zb));
     LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
-    LMM_CK(cudaMemcpyAsync(e->z32.p, z, zb, cudaMemcpyHostToDevice, e->stream));
-    LMM_TRY(run_f32(e, Mode::Fused, e->z32.as<float>(), 0, 0, false, paths, nullptr, nullptr,
-                    e->out.as<double>(), e->se.as<double>()));
+    if (e->nscen == 1 && paths >= kPipelineMinPaths) {
+        LMM_TRY(run_f32_host_pipelined(e, z, paths));
+    } else {
+        LMM_CK(cudaMemcpyAsync(e->z32.p, z, zb, cudaMemcpyHostToDevice, e->stream));
+        LMM_TRY(run_f32(e, Mode::Fused, e->z32.as<float>(), 0, 0, false, paths, nullptr, nullptr,
+                        e->out.as<double>(), e->se.as<double>()));
+    }
     return fetch(e, 1 + 2 * e->nn, out, se);
 }
 

@@ -45,20 +45,33 @@
 #define LMM_TPP_MINB 4
 #endif
 #ifndef LMM_TPP_SEGF
-#define LMM_TPP_SEGF 8
+#define LMM_TPP_SEGF 1
 #endif
 #ifndef LMM_TPP_SEGR
-#define LMM_TPP_SEGR 5
+#define LMM_TPP_SEGR 1
 #endif
 // Reverse steps processed together as a skewed wavefront (independent
 // reconstruction chains per instruction stream): 2 or 4.
 #ifndef LMM_TPP_SKEW
-#define LMM_TPP_SKEW 4
+#define LMM_TPP_SKEW 2
 #endif
 // 1: arrange the reverse cell so that only FFMA -> ex2 -> FFMA -> rcp -> FFMA
 // sits on the reconstruction chain (three more instructions per cell).
 #ifndef LMM_TPP_SHORT
 #define LMM_TPP_SHORT 0
+#endif
+// 0: one unrolled body per step segment (LMM_TPP_SEGF/SEGR). k > 0: a single
+// forward and a single reverse body, entered (forward) or left (reverse) at
+// k-rate chunk boundaries, so the code stays small; each chunk is straight-line.
+#ifndef LMM_TPP_CHUNK
+#define LMM_TPP_CHUNK 8
+#endif
+// 1 (with LMM_TPP_CHUNK > 0): in a reverse group, cell (n-g, i+g) uses the
+// maturity constants and vega row of j = i+2g in step n's numbering, so each
+// constant is loaded once per G cells and each vega row gets one
+// read-modify-write per G cells (partial sums kept in registers).
+#ifndef LMM_TPP_WINDOW
+#define LMM_TPP_WINDOW 0
 #endif
 
 
@@ -279,6 +292,123 @@ __device__ __forceinline__ void column_reduce(const float *vg, int warp, int lan
     }
 }
 
+// One forward step with a single body: rates are grouped in chunks of CH,
+// and the step starts at the chunk holding its first active rate n+1 (cells
+// of that chunk with i <= n are no-ops).
+template <int NN, int CH>
+__device__ __forceinline__ float fwd_step_chunked(float (&L)[NN], const float4 *kcn, float sqez,
+                                                  float delta, int n)
+{
+    float V = 0.0f;
+    const int c0 = (n + 1) / CH;
+#pragma unroll
+    for (int c = 0; c * CH < NN; ++c) {
+        if (c >= c0) {
+#pragma unroll
+            for (int i = (c * CH < 1 ? 1 : c * CH); i < (c + 1) * CH && i < NN; ++i) {
+                const float4 k = kcn[i];
+                const float r = rcp_approx(fmaf(delta, L[i], 1.0f));
+                V = fmaf(k.z, L[i] * r, V);
+                L[i] *= ex2_approx(fmaf(k.x, V + sqez, k.y));
+            }
+        }
+    }
+    return V;
+}
+
+// A group of G reverse steps n..n-G+1 with a single body over positions
+// NN-1 .. -(G-1) (cell (n-g, i+g) at position i), left at the first chunk of
+// CH positions lying wholly below the lowest active position n-2G+3.
+template <int NN, int B, int G, int CH>
+__device__ __forceinline__ void rev_group_chunked(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
+                                                  float delta, float d2, int n)
+{
+    const int imin = n - 2 * G + 3;
+#pragma unroll
+    for (int q = 0; q * CH < NN + G - 1; ++q) {
+        const int top = NN - 1 - q * CH;
+        if (top < imin) break;
+#pragma unroll
+        for (int i = top; i > top - CH && i >= -(G - 1); --i) {
+#pragma unroll
+            for (int g = 0; g < G; ++g)
+                if (i + g >= 1 && i + g <= NN - 1) rev_cell<NN, B>(L, Pb, st[g], i + g, delta, d2);
+        }
+    }
+}
+
+// Reverse cell with its constants and vega accumulator passed in (window form).
+template <int NN>
+__device__ __forceinline__ void rev_cell_w(float (&L)[NN], float (&Pb)[NN], RevStep &s, int i,
+                                           const float4 &k, float dlk, float &acc, float delta)
+{
+    const float y = s.V + s.sqez;
+    const float Ln = L[i] * ex2_approx(-fmaf(k.x, y, k.y));
+    const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
+    const float t = Ln * r;
+    s.V = fmaf(-k.z, t, s.V);
+    const float pb = Pb[i];
+    s.S = fmaf(k.z, pb, s.S);
+    const float tS = t * s.S;
+    acc += fmaf(pb, y - dlk, tS);
+    Pb[i] = fmaf(k.w * r, tS, pb);
+    L[i] = Ln;
+}
+
+// Window form of rev_group_chunked. With j = i+2g, the constants of cell
+// (n-g, i+g) are st[0].kc[j] and its vega row is st[0].vg[j*B] (k = j-n-1
+// of step n): C/D/A[j] hold them for the 2(G-1)+1 positions j is in use. A
+// vega row is valid (k >= 0) for all or none of its G contributors, and all
+// contributors of a valid row sit at or above the lowest active position, so
+// leaving at a chunk boundary after flushing the open rows is exact.
+template <int NN, int B, int G, int CH>
+__device__ __forceinline__ void rev_group_window(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
+                                                 float delta, int n)
+{
+    constexpr int JMAX = NN + G - 2;
+    const float4 *kc = st[0].kc;
+    const float *kx = st[0].kx;
+    float *vg = st[0].vg;
+    float4 C[JMAX + 1];
+    float D[JMAX + 1], A[JMAX + 1];
+#pragma unroll
+    for (int j = NN; j <= JMAX; ++j) {
+        C[j] = kc[j];
+        D[j] = kx[j];
+        A[j] = 0.0f;
+    }
+    const int imin = n - 2 * G + 3;
+#pragma unroll
+    for (int q = 0; q * CH < NN + G - 1; ++q) {
+        const int top = NN - 1 - q * CH;
+        if (top < imin) {
+#pragma unroll
+            for (int j = top + 1; j <= top + 2 * (G - 1); ++j)
+                if (j >= 1 && j <= JMAX) vg[j * B] += A[j];
+            return;
+        }
+#pragma unroll
+        for (int i = top; i > top - CH && i >= -(G - 1); --i) {
+            if (i >= 1) {
+                C[i] = kc[i];
+                D[i] = kx[i];
+                A[i] = 0.0f;
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (i + g >= 1 && i + g <= NN - 1) {
+                    const int j = i + 2 * g;
+                    rev_cell_w<NN>(L, Pb, st[g], i + g, C[j], D[j], A[j], delta);
+                }
+            }
+            const int jf = i + 2 * (G - 1);
+            if (jf >= 1 && jf <= JMAX) vg[jf * B] += A[jf];
+        }
+    }
+#pragma unroll
+    for (int j = 1; j <= G - 2; ++j) vg[j * B] += A[j];
+}
+
 // Forward over all steps, segment by segment (segment s: steps [lo, hi),
 // body over rates lo+1..NN-1).
 template <int NN, int NMAT, int SEG, bool PHILOX, Mode MODE, int S = 0>
@@ -296,7 +426,11 @@ __device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, f
                 if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
             }
             const float sqez = sqd * pick4(zq, n & 3);
+#if LMM_TPP_CHUNK > 0
+            const float V = fwd_step_chunked<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez, delta, n);
+#else
             const float V = fwd_step<NN, lo + 1>(L, kc0 - (n + 1), sqez, delta);
+#endif
             if (MODE == Mode::Fused)
                 vt_s[n * B] = V;
             else if (active)
@@ -336,7 +470,13 @@ __device__ __forceinline__ void reverse_all(float (&L)[NN], float (&Pb)[NN], con
                 st[g].kx = kx0 - (m + 1);
                 st[g].vg = vg0 - (m + 1) * B;
             }
+#if LMM_TPP_CHUNK > 0 && LMM_TPP_WINDOW
+            rev_group_window<NN, B, G, LMM_TPP_CHUNK>(L, Pb, st, delta, n);
+#elif LMM_TPP_CHUNK > 0
+            rev_group_chunked<NN, B, G, LMM_TPP_CHUNK>(L, Pb, st, delta, d2, n);
+#else
             rev_group<NN, B, lo + 1, G>(L, Pb, st, delta, d2);
+#endif
         }
         reverse_all<NN, NMAT, SEG, PHILOX, MODE, S - 1>(L, Pb, kc0, kx0, vg0, zq, zq_next, zp, seed,
                                                         gpath, sqd, delta, d2, vt_s, tape_v, total);

@@ -115,7 +115,9 @@ int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops);
 /* ---- value + all Greeks, FP32 adjoint (the fast path) ----------------- */
 /* Replaces the per-path work of liborSwaptionGreeks.cpp:281-344 (forward,
  * payoff adjoint, reverse sweep) plus the vega adjoint, for every path, with
- * FP64 cross-path sums. Oracle mode: normals read from memory. */
+ * FP64 cross-path sums. Oracle mode: normals read from memory. The host call
+ * overlaps the host->device copy of z with the computation (z in pinned
+ * memory gets the full copy bandwidth). */
 int lmm_greeks_f32_host(lmm_engine *e, const float *z, int64_t paths, double *out, double *se);
 int lmm_greeks_f32_device(lmm_engine *e, const float *d_z, int64_t paths, double *d_out,
                           double *d_se);

@@ -317,3 +317,63 @@ def test_fp32_range_is_never_silently_wrong(P):
             assert_f32_close(g[0], m, cfg.nn, "200x150 lambda=0.35")
         g64, _ = e.greeks_f64(z.astype(np.float64))
     np.testing.assert_allclose(g64[0], m, rtol=1e-9, atol=1e-10 * np.abs(m).max())
+
+
+def test_pipelined_host_call_equals_device_call(P):
+    """lmm_greeks_f32_host overlaps chunked copies with per-chunk kernels above
+    2^18 paths; it must agree with the single-launch device call."""
+    import torch
+    cfg = cfgs().workload(2, 300_001)
+    z = O.normals_f32(17, cfg.paths, cfg.nmat)
+    dz = torch.from_numpy(z).cuda()
+    out = torch.zeros(cfg.nout, dtype=torch.float64, device="cuda")
+    with P.Engine(cfg) as e:
+        g, gse = e.greeks_f32(z)
+        assert e.last_launches == 5                 # 4 chunk kernels + finalize
+        e.greeks_f32_device(dz.data_ptr(), cfg.paths, out.data_ptr())
+        e.synchronize()
+    d = out.cpu().numpy()
+    # Chunk boundaries regroup which 32 paths share a warp's FP32 column sums,
+    # so the two calls differ by summation order only (~1e-8 relative).
+    np.testing.assert_allclose(g[0], d, rtol=1e-7, atol=1e-9 * np.abs(d).max())
+
+
+def test_full_size_long_tenor_fp32_vs_fp64(P):
+    """Workload 3 at its named size (1,048,576 paths, NN=160, NMAT=120,
+    checkpoints every 8 steps) against the FP64 kernel on identical normals."""
+    import torch
+    cfg = cfgs().workload(3)
+    n = cfg.paths
+    dz = torch.empty(n * cfg.nmat, dtype=torch.float32, device="cuda")
+    P.normals_f32_device(3, n, cfg.nmat, dz.data_ptr())
+    dz64 = dz.double()
+    o32 = torch.zeros(cfg.nout, dtype=torch.float64, device="cuda")
+    o64 = torch.zeros_like(o32)
+    with P.Engine(cfg) as e:
+        e.greeks_f32_device(dz.data_ptr(), n, o32.data_ptr())
+        e.greeks_f64_device(dz64.data_ptr(), n, o64.data_ptr())
+        e.synchronize()
+    assert_f32_close(o32.cpu().numpy(), o64.cpu().numpy(), cfg.nn, "workload 3 full size")
+
+
+def test_full_size_scenario_sweep_consistent(P):
+    """Workload 5 at its named size (256 curves x 262,144 paths, one launch):
+    every scenario finite, and three of them equal to single-curve runs."""
+    import torch
+    cfg = cfgs().workload(5)
+    n = cfg.paths
+    dz = torch.empty(n * cfg.nmat, dtype=torch.float32, device="cuda")
+    P.normals_f32_device(5, n, cfg.nmat, dz.data_ptr())
+    out = torch.zeros(cfg.nscen * cfg.nout, dtype=torch.float64, device="cuda")
+    with P.Engine(cfg) as e:
+        e.greeks_f32_device(dz.data_ptr(), n, out.data_ptr())
+        e.synchronize()
+    g = out.cpu().numpy().reshape(cfg.nscen, cfg.nout)
+    assert np.all(np.isfinite(g))
+    for s in (0, 101, 255):
+        one = torch.zeros(cfg.nout, dtype=torch.float64, device="cuda")
+        with P.Engine(cfg.scenario(s)) as e1:
+            e1.greeks_f32_device(dz.data_ptr(), n, one.data_ptr())
+            e1.synchronize()
+        r = one.cpu().numpy()
+        np.testing.assert_allclose(g[s], r, rtol=1e-9, atol=1e-12 * np.abs(r).max())
