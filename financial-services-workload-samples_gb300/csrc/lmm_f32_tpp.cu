@@ -71,7 +71,7 @@
 // constant is loaded once per G cells and each vega row gets one
 // read-modify-write per G cells (partial sums kept in registers).
 #ifndef LMM_TPP_WINDOW
-#define LMM_TPP_WINDOW 0
+#define LMM_TPP_WINDOW 1
 #endif
 
 
