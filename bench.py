@@ -284,6 +284,34 @@ def run_ours(args):
                "tolerance": 1e-4, "rule": "|f32-f64| / max(|f64|, 1% of the largest of its group)",
                "max_abs_err_over_mc_se": float(np.max(np.abs(res32 - r64) / np.maximum(se32, 1e-300)))}
 
+    # ---- phase split: forward (+payoff, tape write) and backward (tape read,
+    # payoff adjoint, reverse sweep) as separate calls of the C-ABI pair --------
+    phases = None
+    if rank == 0 and not args.skip_phases:
+        tape = eng.tape(n)
+        val = torch.zeros(1, dtype=torch.float64, device=dev)
+        grad = torch.zeros(2 * cfg.nn, dtype=torch.float64, device=dev)
+
+        def med_ms(f, k=5):
+            for _ in range(2):
+                f()
+            eng.set_timing(True)
+            ts = []
+            for _ in range(k):
+                f()
+                ts.append(eng.kernel_time()[0])
+            eng.set_timing(False)
+            return statistics.median(ts)
+
+        fw = med_ms(lambda: eng.forward_f32_device(dz.data_ptr(), n, tape, val.data_ptr()))
+        bw = med_ms(lambda: eng.backward_f32_device(dz.data_ptr(), tape, [1.0], grad.data_ptr()))
+        tape.close()
+        phases = {"forward_ms": fw, "backward_ms": bw, "fused_ms": statistics.median(kern_ms),
+                  "tape_bytes": 4 * (cfg.nn + nmat) * n,
+                  "note": "forward = Euler steps + payoff + tape write (terminal rates, per-step drift "
+                          "sums); backward = tape read + payoff adjoint + reverse sweep; the fused "
+                          "kernel keeps both in registers and shared memory"}
+
     # ---- FP64 bump-and-revalue comparator on a bounded sample -------------
     bump = None
     if rank == 0 and not args.skip_bump:
@@ -359,7 +387,8 @@ def run_ours(args):
             "e2e": {"value": e2e, "unit": "paths/s", "h2d_bytes_per_step": 4 * n * nmat,
                     "d2h_bytes_per_step": 2 * 8 * nout + 4, "launches_per_step": e2e_launches,
                     "api": "lmm_greeks_f32_host (pinned host normals)"},
-            "roofline": roof, "clocks": clk.summary(), "accuracy": acc, "fp64_bump_comparator": bump,
+            "roofline": roof, "clocks": clk.summary(), "accuracy": acc, "phase_split": phases,
+            "fp64_bump_comparator": bump,
             "other_workloads": others}
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline_port(cfg, target_s=args.cpu_seconds)
@@ -387,6 +416,7 @@ def main():
     ap.add_argument("--skip-bump", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-others", action="store_true")
+    ap.add_argument("--skip-phases", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -615,10 +615,15 @@ int lmm_greeks_f32_device(lmm_engine *e, const float *d_z, int64_t paths, double
 
 // Host call with the copy overlapped: the normals go up in kHostChunks
 // pieces on the engine's copy stream; the fused kernel of piece c starts as
-// soon as piece c has landed, while piece c+1 is still in flight. Each piece
-// writes its own range of partial sums and one ordered k_finalize covers them
-// all. Single-scenario engines only.
-constexpr int kHostChunks = 4;
+// soon as piece c has landed, while piece c+1 is still in flight (relative
+// piece sizes kHostSplit). Each piece writes its own range of partial sums
+// and one ordered k_finalize covers them all. Single-scenario engines only.
+#ifndef LMM_HOST_SPLIT
+#define LMM_HOST_SPLIT 1, 1, 1, 1
+#endif
+constexpr int kHostSplit[] = {LMM_HOST_SPLIT};
+constexpr int kHostChunks = sizeof(kHostSplit) / sizeof(kHostSplit[0]);
+static_assert(kHostChunks <= 8, "one copy event per piece");
 constexpr int64_t kPipelineMinPaths = int64_t(1) << 18;
 
 int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
@@ -632,10 +637,12 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
     const int nout = 1 + 2 * e->nn;
     const int C = kHostChunks;
     int64_t cpaths[kHostChunks], cfirst[kHostChunks], citems[kHostChunks], cppt[kHostChunks];
-    int64_t total_items = 0;
+    int64_t total_items = 0, wsum = 0, wcum = 0;
+    for (int c = 0; c < C; ++c) wsum += kHostSplit[c];
     for (int c = 0; c < C; ++c) {
-        cfirst[c] = paths * c / C;
-        cpaths[c] = paths * (c + 1) / C - cfirst[c];
+        cfirst[c] = paths * wcum / wsum;
+        wcum += kHostSplit[c];
+        cpaths[c] = paths * wcum / wsum - cfirst[c];
         plan_items(e, 1, cpaths[c], per_batch, bps, &citems[c], &cppt[c]);
         if (cppt[c] > INT32_MAX || citems[c] > INT32_MAX) return fail(LMM_ERR_TOO_LARGE, "launch too large");
         total_items += citems[c];

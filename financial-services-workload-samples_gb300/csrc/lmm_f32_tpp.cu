@@ -11,10 +11,11 @@
 // Branch-free steps. Step n moves rates i > n only. The per-maturity
 // constants are stored with NMAT zero entries in front (k = i-n-1 < 0), so a
 // cell with i <= n multiplies L by 2^0 = 1 and adds 0 to every running sum:
-// it is an exact no-op. Each step is then one straight-line block over rates
-// I0..NN-1 that the compiler can schedule across cells; the steps are split
-// into SEG segments with their own I0 (= first step of the segment + 1) so
-// that only a few no-op cells run per step.
+// it is an exact no-op. The forward and the reverse each have ONE unrolled
+// body over the rates, cut into chunks of LMM_TPP_CHUNK rates: a step enters
+// (forward) or leaves (reverse) the body at the chunk holding its first
+// active rate, so at most CHUNK-1 no-op cells run per step and the code stays
+// small enough for the instruction cache.
 //
 // Reverse sweep without a stored trajectory. With V_i the inclusive drift sum
 // of step n (saved per step by the forward), the Euler step runs backwards,
@@ -30,7 +31,12 @@
 // (k < 0) are NMAT spare rows per thread that are never read.
 // The reconstruction is a serial chain (exp -> rcp -> drift sum) per step, so
 // steps are processed as a skewed wavefront: cell (n,i) next to cell
-// (n-1,i+1) (and (n-2,i+2), ...), independent chains in one instruction stream.
+// (n-1,i+1), independent chains in one instruction stream. Within such a
+// pair, cell (n-1, i+1) uses the constants and vega row that cell (n, i+2)
+// used two positions earlier; they are kept in registers (rev_group_window),
+// so each constant is read from shared memory once and each vega row gets one
+// read-modify-write per two cells. The fused forward pairs steps the same way
+// (fwd_pair_window).
 //
 // Cross-path reduction: per warp, each lane sums one output column over the
 // warp's 32 paths (shared-memory transpose), then adds into per-warp FP64
@@ -72,6 +78,16 @@
 // read-modify-write per G cells (partial sums kept in registers).
 #ifndef LMM_TPP_WINDOW
 #define LMM_TPP_WINDOW 1
+#endif
+// 1 (with LMM_TPP_CHUNK > 0): forward steps in skewed pairs sharing each
+// constant load (fwd_pair_window).
+#ifndef LMM_TPP_FWD_PAIR
+#define LMM_TPP_FWD_PAIR 1
+#endif
+// 1: the window reverse cell forms y - delta*lambda_k with an FMA instead of
+// reading delta*lambda_k from a table.
+#ifndef LMM_TPP_WIN_NOKX
+#define LMM_TPP_WIN_NOKX 1
 #endif
 
 
@@ -316,6 +332,48 @@ __device__ __forceinline__ float fwd_step_chunked(float (&L)[NN], const float4 *
     return V;
 }
 
+// One forward cell (path_calc_b1 :66-72): drift sum and rate update.
+__device__ __forceinline__ void fwd_cell(float &L, float &V, const float4 &k, float sqez, float delta)
+{
+    const float r = rcp_approx(fmaf(delta, L, 1.0f));
+    V = fmaf(k.z, L * r, V);
+    L *= ex2_approx(fmaf(k.x, V + sqez, k.y));
+}
+
+// Forward steps n and n+1 with one body over positions p (ascending): cell
+// (n, p) and cell (n+1, p-1). The second finds L_{n+1,p-1} written by cell
+// (n, p-1) one position earlier, so the two drift chains are independent
+// within a position. Cell (n+1, p-1) has k = p-n-3, the constants loaded for
+// cell (n, p-2), so each constant is loaded once per two cells (C[] keeps
+// three). Entered at the chunk holding rate n+1; step n+1's cells below its
+// first active rate n+2 see zero constants and are exact no-ops.
+template <int NN, int CH>
+__device__ __forceinline__ void fwd_pair_window(float (&L)[NN], const float4 *kcn, float sqez0,
+                                                float sqez1, float delta, int n, float &V0, float &V1)
+{
+    float4 C[3];  // ring: C[j % 3] holds the constants of position j
+    V0 = 0.0f;
+    V1 = 0.0f;
+    const int c0 = (n + 1) / CH;
+#pragma unroll
+    for (int c = 0; c * CH < NN; ++c) {
+        if (c >= c0) {
+            if (c == c0) {
+#pragma unroll
+                for (int j = c * CH - 2; j < c * CH; ++j)
+                    if (j >= 0) C[j % 3] = kcn[j];
+            }
+#pragma unroll
+            for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
+                C[p % 3] = kcn[p];
+                if (p >= 1) fwd_cell(L[p], V0, C[p % 3], sqez0, delta);
+                if (p - 1 >= 1) fwd_cell(L[p - 1], V1, C[(p + 1) % 3], sqez1, delta);
+            }
+        }
+    }
+    fwd_cell(L[NN - 1], V1, C[(NN - 2) % 3], sqez1, delta);
+}
+
 // A group of G reverse steps n..n-G+1 with a single body over positions
 // NN-1 .. -(G-1) (cell (n-g, i+g) at position i), left at the first chunk of
 // CH positions lying wholly below the lowest active position n-2G+3.
@@ -350,63 +408,63 @@ __device__ __forceinline__ void rev_cell_w(float (&L)[NN], float (&Pb)[NN], RevS
     const float pb = Pb[i];
     s.S = fmaf(k.z, pb, s.S);
     const float tS = t * s.S;
+#if LMM_TPP_WIN_NOKX
+    acc += fmaf(pb, fmaf(-delta, k.w, y), tS);
+#else
     acc += fmaf(pb, y - dlk, tS);
+#endif
     Pb[i] = fmaf(k.w * r, tS, pb);
     L[i] = Ln;
 }
 
 // Window form of rev_group_chunked. With j = i+2g, the constants of cell
 // (n-g, i+g) are st[0].kc[j] and its vega row is st[0].vg[j*B] (k = j-n-1
-// of step n): C/D/A[j] hold them for the 2(G-1)+1 positions j is in use. A
+// of step n): C/D/A hold them from position j (load) to position j-2(G-1)
+// (last use, vega flush), in rings of 2G-1 slots indexed j mod (2G-1). A
 // vega row is valid (k >= 0) for all or none of its G contributors, and all
-// contributors of a valid row sit at or above the lowest active position, so
-// leaving at a chunk boundary after flushing the open rows is exact.
+// contributors of a valid row sit at or above the lowest active position
+// n-2G+3, so leaving at a chunk boundary below it is exact: the rows still
+// open then are spare rows (k < 0), which are never read.
 template <int NN, int B, int G, int CH>
 __device__ __forceinline__ void rev_group_window(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
                                                  float delta, int n)
 {
     constexpr int JMAX = NN + G - 2;
+    constexpr int W = 2 * G - 1;
     const float4 *kc = st[0].kc;
     const float *kx = st[0].kx;
     float *vg = st[0].vg;
-    float4 C[JMAX + 1];
-    float D[JMAX + 1], A[JMAX + 1];
+    float4 C[W];
+    float D[W], A[W];
 #pragma unroll
     for (int j = NN; j <= JMAX; ++j) {
-        C[j] = kc[j];
-        D[j] = kx[j];
-        A[j] = 0.0f;
+        C[j % W] = kc[j];
+        D[j % W] = LMM_TPP_WIN_NOKX ? 0.0f : kx[j];
+        A[j % W] = 0.0f;
     }
     const int imin = n - 2 * G + 3;
 #pragma unroll
     for (int q = 0; q * CH < NN + G - 1; ++q) {
         const int top = NN - 1 - q * CH;
-        if (top < imin) {
-#pragma unroll
-            for (int j = top + 1; j <= top + 2 * (G - 1); ++j)
-                if (j >= 1 && j <= JMAX) vg[j * B] += A[j];
-            return;
-        }
+        if (top < imin) return;
 #pragma unroll
         for (int i = top; i > top - CH && i >= -(G - 1); --i) {
             if (i >= 1) {
-                C[i] = kc[i];
-                D[i] = kx[i];
-                A[i] = 0.0f;
+                C[i % W] = kc[i];
+                D[i % W] = LMM_TPP_WIN_NOKX ? 0.0f : kx[i];
+                A[i % W] = 0.0f;
             }
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 if (i + g >= 1 && i + g <= NN - 1) {
                     const int j = i + 2 * g;
-                    rev_cell_w<NN>(L, Pb, st[g], i + g, C[j], D[j], A[j], delta);
+                    rev_cell_w<NN>(L, Pb, st[g], i + g, C[j % W], D[j % W], A[j % W], delta);
                 }
             }
             const int jf = i + 2 * (G - 1);
-            if (jf >= 1 && jf <= JMAX) vg[jf * B] += A[jf];
+            if (jf >= 1 && jf <= JMAX) vg[jf * B] += A[jf % W];
         }
     }
-#pragma unroll
-    for (int j = 1; j <= G - 2; ++j) vg[j * B] += A[j];
 }
 
 // Forward over all steps, segment by segment (segment s: steps [lo, hi),
@@ -420,21 +478,44 @@ __device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, f
     if constexpr (S < SEG) {
         constexpr int lo = S * NMAT / SEG, hi = (S + 1) * NMAT / SEG;
         constexpr int B = kTppBlock;
-        for (int n = lo; n < hi; ++n) {
-            if ((n & 3) == 0) {
-                zq = zq_next;
-                if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
-            }
-            const float sqez = sqd * pick4(zq, n & 3);
-#if LMM_TPP_CHUNK > 0
-            const float V = fwd_step_chunked<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez, delta, n);
+#if LMM_TPP_CHUNK > 0 && LMM_TPP_FWD_PAIR
+        // Paired steps in the fused kernel only: in the forward-only kernel the
+        // pair's extra live constants cost more occupancy than they save.
+        constexpr bool pair = MODE == Mode::Fused;
 #else
-            const float V = fwd_step<NN, lo + 1>(L, kc0 - (n + 1), sqez, delta);
+        constexpr bool pair = false;
 #endif
-            if (MODE == Mode::Fused)
-                vt_s[n * B] = V;
-            else if (active)
-                tape_v[(int64_t)n * total] = V;
+        if constexpr (pair) {
+            static_assert(SEG == 1 && NMAT % 2 == 0, "paired forward steps run over all steps");
+            for (int n = 0; n < NMAT; n += 2) {
+                if ((n & 3) == 0) {
+                    zq = zq_next;
+                    if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+                }
+                const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
+                const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
+                float V0, V1;
+                fwd_pair_window<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez0, sqez1, delta, n, V0, V1);
+                vt_s[n * B] = V0;
+                vt_s[(n + 1) * B] = V1;
+            }
+        } else {
+            for (int n = lo; n < hi; ++n) {
+                if ((n & 3) == 0) {
+                    zq = zq_next;
+                    if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+                }
+                const float sqez = sqd * pick4(zq, n & 3);
+#if LMM_TPP_CHUNK > 0
+                const float V = fwd_step_chunked<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez, delta, n);
+#else
+                const float V = fwd_step<NN, lo + 1>(L, kc0 - (n + 1), sqez, delta);
+#endif
+                if (MODE == Mode::Fused)
+                    vt_s[n * B] = V;
+                else if (active)
+                    tape_v[(int64_t)n * total] = V;
+            }
         }
         forward_all<NN, NMAT, SEG, PHILOX, MODE, S + 1>(L, kc0, zq, zq_next, zp, seed, gpath, sqd,
                                                         delta, vt_s, tape_v, total, active);
