@@ -312,6 +312,39 @@ def run_ours(args):
                           "sums); backward = tape read + payoff adjoint + reverse sweep; the fused "
                           "kernel keeps both in registers and shared memory"}
 
+    # ---- the MRG32k3a/AS241 normal stream (the reference's generator family):
+    # the workload's normals generated on the device vs the oracle on one core
+    rng = None
+    if rank == 0 and not args.skip_rng:
+        from oracle import oracle as O
+        cnt = n * nmat
+        zr = torch.empty(cnt, dtype=torch.float64, device=dev)
+        rates = {}
+        for kind, buf in (("f32", dz), ("f64", zr)):
+            fn = P.mrg32k3a_normals_f32_device if kind == "f32" else P.mrg32k3a_normals_f64_device
+            fn(12345, 0, cnt, buf.data_ptr(), stream=stream.cuda_stream)
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            for _ in range(3):
+                fn(12345, 0, cnt, buf.data_ptr(), stream=stream.cuda_stream)
+            g1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = g0.elapsed_time(g1) / 3
+            rates[kind] = {"normals_per_s": cnt / (ms * 1e-3), "ms": ms,
+                           "output_gbs": cnt * buf.element_size() / (ms * 1e-3) / 1e9}
+        del zr
+        ns = 2_000_000
+        t0 = time.perf_counter()
+        O.mrg32k3a_normals_f64(12345, 0, ns)
+        cpu_rate = ns / (time.perf_counter() - t0)
+        rng = {"count": cnt, "device": rates, "cpu_oracle_normals_per_s_1core": cpu_rate,
+               "note": "MRG32k3a (L'Ecuyer 1999) with skip-ahead, AS241 inversion (PPND16 FP64, PPND7 FP32); "
+                       "FP64 output computed in FP64 (GB300 FP64 rate), FP32 output by PPND7 in FP32"}
+        # restore the bench's Philox normals in dz (overwritten above)
+        P.normals_f32_device(20260603, n, nmat, dz.data_ptr(), stream=stream.cuda_stream,
+                             path0=rank_path0(rank, n))
+        torch.cuda.synchronize(dev)
+
     # ---- FP64 bump-and-revalue comparator on a bounded sample -------------
     bump = None
     if rank == 0 and not args.skip_bump:
@@ -388,6 +421,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": 2 * 8 * nout + 4, "launches_per_step": e2e_launches,
                     "api": "lmm_greeks_f32_host (pinned host normals)"},
             "roofline": roof, "clocks": clk.summary(), "accuracy": acc, "phase_split": phases,
+            "rng_mrg32k3a": rng,
             "fp64_bump_comparator": bump,
             "other_workloads": others}
     if rank == 0 and not args.skip_cpu:
@@ -417,6 +451,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-others", action="store_true")
     ap.add_argument("--skip-phases", action="store_true")
+    ap.add_argument("--skip-rng", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -33,6 +33,8 @@ EXPORTS = (
     "lmm_greeks_f64_host", "lmm_greeks_f64_device", "lmm_bump_greeks_f64_device",
     "lmm_bump_greeks_f64_host", "lmm_normals_f32_device", "lmm_normals_f64_device",
     "lmm_swaption_greeks", "lmm_swaption_greeks_f32", "lmm_greeks_f32_device_noalloc",
+    "lmm_mrg32k3a_uniforms_device", "lmm_mrg32k3a_normals_f64_device", "lmm_mrg32k3a_normals_f32_device",
+    "lmm_swaption_greeks_mrg32k3a", "lmm_swaption_greeks_mrg32k3a_f32",
 )
 
 
@@ -99,6 +101,13 @@ def lib():
         "lmm_swaption_greeks": ([dp, C.c_int, C.c_double, C.c_double, C.c_int, dp, dp, C.c_int], C.c_int),
         "lmm_swaption_greeks_f32": ([fp, C.c_int, C.c_float, C.c_float, C.c_int, fp, fp, C.c_int], C.c_int),
         "lmm_greeks_f32_device_noalloc": ([P, vp, i64, vp, vp, vp], C.c_int),
+        "lmm_mrg32k3a_uniforms_device": ([C.c_uint32, i64, i64, vp, vp], C.c_int),
+        "lmm_mrg32k3a_normals_f64_device": ([C.c_uint32, i64, i64, C.c_double, C.c_double, vp, vp], C.c_int),
+        "lmm_mrg32k3a_normals_f32_device": ([C.c_uint32, i64, i64, C.c_float, C.c_float, vp, vp], C.c_int),
+        "lmm_swaption_greeks_mrg32k3a": ([dp, C.c_int, C.c_double, C.c_double, C.c_int, dp, dp, C.c_int],
+                                         C.c_int),
+        "lmm_swaption_greeks_mrg32k3a_f32": ([fp, C.c_int, C.c_float, C.c_float, C.c_int, fp, fp, C.c_int],
+                                             C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -292,18 +301,41 @@ def normals_f64_device(seed: int, paths: int, nmat: int, d_z: int, stream: int =
            "lmm_normals_f64_device")
 
 
-def swaption_greeks(num_paths: int, mean: float = 0.0, std_dev: float = 1.0, seed: int = 1234):
-    """The reference's liborSwaptionGreeks call (FP64). Returns (z, d_v, d_Lb)."""
+def mrg32k3a_uniforms_device(seed: int, first: int, count: int, d_u: int, stream: int = 0):
+    """Stream elements [first, first+count) of MRG32k3a as FP64 uniforms in (0,1)."""
+    _check(lib().lmm_mrg32k3a_uniforms_device(seed, first, count, d_u, stream or None),
+           "lmm_mrg32k3a_uniforms_device")
+
+
+def mrg32k3a_normals_f64_device(seed: int, first: int, count: int, d_z: int, stream: int = 0,
+                                mean: float = 0.0, sd: float = 1.0):
+    _check(lib().lmm_mrg32k3a_normals_f64_device(seed, first, count, mean, sd, d_z, stream or None),
+           "lmm_mrg32k3a_normals_f64_device")
+
+
+def mrg32k3a_normals_f32_device(seed: int, first: int, count: int, d_z: int, stream: int = 0,
+                                mean: float = 0.0, sd: float = 1.0):
+    _check(lib().lmm_mrg32k3a_normals_f32_device(seed, first, count, mean, sd, d_z, stream or None),
+           "lmm_mrg32k3a_normals_f32_device")
+
+
+def swaption_greeks(num_paths: int, mean: float = 0.0, std_dev: float = 1.0, seed: int = 1234,
+                    rng: str = "philox"):
+    """The reference's liborSwaptionGreeks call (FP64). Returns (z, d_v, d_Lb).
+    rng = "mrg32k3a" draws z from the MRG32k3a/AS241 stream instead."""
     z = np.zeros(40 * num_paths)
     v, lb = C.c_double(), C.c_double()
-    _check(lib().lmm_swaption_greeks(_dp(z), 40 * num_paths, mean, std_dev, seed, C.byref(v), C.byref(lb),
-                                     num_paths), "lmm_swaption_greeks")
+    name = {"philox": "lmm_swaption_greeks", "mrg32k3a": "lmm_swaption_greeks_mrg32k3a"}[rng]
+    _check(getattr(lib(), name)(_dp(z), 40 * num_paths, mean, std_dev, seed, C.byref(v), C.byref(lb),
+                                num_paths), name)
     return z, v.value, lb.value
 
 
-def swaption_greeks_f32(num_paths: int, mean: float = 0.0, std_dev: float = 1.0, seed: int = 1234):
+def swaption_greeks_f32(num_paths: int, mean: float = 0.0, std_dev: float = 1.0, seed: int = 1234,
+                        rng: str = "philox"):
     z = np.zeros(40 * num_paths, dtype=np.float32)
     v, lb = C.c_float(), C.c_float()
-    _check(lib().lmm_swaption_greeks_f32(_fp(z), 40 * num_paths, mean, std_dev, seed, C.byref(v),
-                                         C.byref(lb), num_paths), "lmm_swaption_greeks_f32")
+    name = {"philox": "lmm_swaption_greeks_f32", "mrg32k3a": "lmm_swaption_greeks_mrg32k3a_f32"}[rng]
+    _check(getattr(lib(), name)(_fp(z), 40 * num_paths, mean, std_dev, seed, C.byref(v),
+                                C.byref(lb), num_paths), name)
     return z, v.value, lb.value

@@ -22,6 +22,8 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "liblmm_gb300.so")
+CLI_SRC = os.path.join(PKG, "cli", "lmm_bench.cpp")
+CLI = os.path.join(PKG, "lmm_bench")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -77,7 +79,23 @@ def build(force: bool = False, jobs: int | None = None, extra=(), verbose: bool 
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    build_cli(force)
     return LIB
+
+
+def build_cli(force: bool = False) -> str:
+    """The benchmark driver (cli/lmm_bench.cpp), linked against the library
+    beside it (rpath $ORIGIN)."""
+    deps = [CLI_SRC, LIB, os.path.join(INCLUDE, "lmm_gb300.h")]
+    if force or not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(d) for d in deps):
+        tmp = CLI + f".tmp{os.getpid()}"
+        cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-Wall", "-Wextra", "-I" + INCLUDE, CLI_SRC,
+               "-L" + PKG, "-llmm_gb300", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"lmm_bench build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":

@@ -837,21 +837,57 @@ int lmm_normals_f64_device(uint64_t seed, int64_t path0, int64_t paths, int32_t 
     return LMM_OK;
 }
 
+static int check_stream_range(int64_t first, int64_t count, const void *out)
+{
+    if (first < 0 || count < 0 || count > INT64_MAX - first)
+        return fail(LMM_ERR_INVALID_ARG, "need first >= 0, count >= 0, first + count < 2^63");
+    if (count > 0 && !out) return fail(LMM_ERR_INVALID_ARG, "output pointer is NULL");
+    return LMM_OK;
+}
+
+int lmm_mrg32k3a_uniforms_device(uint32_t seed, int64_t first, int64_t count, double *d_u, void *stream)
+{
+    LMM_TRY(check_stream_range(first, count, d_u));
+    LMM_CK(lmm::launch_mrg32k3a(0, seed, first, count, 0.0, 1.0, d_u, static_cast<cudaStream_t>(stream)));
+    return LMM_OK;
+}
+
+int lmm_mrg32k3a_normals_f64_device(uint32_t seed, int64_t first, int64_t count, double mean,
+                                    double std_dev, double *d_z, void *stream)
+{
+    LMM_TRY(check_stream_range(first, count, d_z));
+    if (!std::isfinite(mean) || !std::isfinite(std_dev)) return fail(LMM_ERR_INVALID_ARG, "mean/std_dev must be finite");
+    LMM_CK(lmm::launch_mrg32k3a(1, seed, first, count, mean, std_dev, d_z, static_cast<cudaStream_t>(stream)));
+    return LMM_OK;
+}
+
+int lmm_mrg32k3a_normals_f32_device(uint32_t seed, int64_t first, int64_t count, float mean,
+                                    float std_dev, float *d_z, void *stream)
+{
+    LMM_TRY(check_stream_range(first, count, d_z));
+    if (!std::isfinite(mean) || !std::isfinite(std_dev)) return fail(LMM_ERR_INVALID_ARG, "mean/std_dev must be finite");
+    LMM_CK(lmm::launch_mrg32k3a(2, seed, first, count, mean, std_dev, d_z, static_cast<cudaStream_t>(stream)));
+    return LMM_OK;
+}
+
 // ---- the reference's signature ----------------------------------------------------
 
-int lmm_swaption_greeks(double *z, int num, double mean, double std_dev, int seed, double *d_v,
-                        double *d_Lb, int numPaths)
+static int swaption_greeks_f64(bool mrg, double *z, int num, double mean, double std_dev, double *d_v,
+                               double *d_Lb, int numPaths)
 {
-    (void)seed;  // ignored, as in the reference (generateRand uses its default key)
     if (!z || !d_v || !d_Lb || numPaths < 1 || (int64_t)num != 40 * (int64_t)numPaths)
         return fail(LMM_ERR_INVALID_ARG, "need z[40*numPaths], d_v, d_Lb and numPaths >= 1");
+    if (!std::isfinite(mean) || !std::isfinite(std_dev)) return fail(LMM_ERR_INVALID_ARG, "mean/std_dev must be finite");
     std::lock_guard<std::mutex> lk(g_ref_mu);
     lmm_engine *e = nullptr;
     LMM_TRY(ref_engine(&e));
     LMM_TRY(set_device(e));
     LMM_TRY(e->z64.ensure(sizeof(double) * (size_t)num));
     LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
-    LMM_CK(lmm::launch_normals_f64(12345u, 0, numPaths, 40, mean, std_dev, e->z64.as<double>(), e->stream));
+    if (mrg)
+        LMM_CK(lmm::launch_mrg32k3a(1, 12345u, 0, num, mean, std_dev, e->z64.p, e->stream));
+    else
+        LMM_CK(lmm::launch_normals_f64(12345u, 0, numPaths, 40, mean, std_dev, e->z64.as<double>(), e->stream));
     LMM_CK(cudaMemcpyAsync(z, e->z64.p, sizeof(double) * (size_t)num, cudaMemcpyDeviceToHost, e->stream));
     LMM_TRY(run_f64(e, e->z64.as<double>(), numPaths, e->out.as<double>(), e->se.as<double>()));
     std::vector<double> out(1 + 2 * e->nn);
@@ -861,10 +897,9 @@ int lmm_swaption_greeks(double *z, int num, double mean, double std_dev, int see
     return LMM_OK;
 }
 
-int lmm_swaption_greeks_f32(float *z, int num, float mean, float std_dev, int seed, float *d_v,
-                            float *d_Lb, int numPaths)
+static int swaption_greeks_f32(bool mrg, float *z, int num, float mean, float std_dev, float *d_v,
+                               float *d_Lb, int numPaths)
 {
-    (void)seed;
     if (!z || !d_v || !d_Lb || numPaths < 1 || (int64_t)num != 40 * (int64_t)numPaths)
         return fail(LMM_ERR_INVALID_ARG, "need z[40*numPaths], d_v, d_Lb and numPaths >= 1");
     if (!std::isfinite(mean) || !std::isfinite(std_dev)) return fail(LMM_ERR_INVALID_ARG, "mean/std_dev must be finite");
@@ -874,7 +909,10 @@ int lmm_swaption_greeks_f32(float *z, int num, float mean, float std_dev, int se
     LMM_TRY(set_device(e));
     LMM_TRY(e->z32.ensure(sizeof(float) * (size_t)num));
     LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
-    LMM_CK(lmm::launch_normals_f32(12345u, 0, numPaths, 40, mean, std_dev, e->z32.as<float>(), e->stream));
+    if (mrg)
+        LMM_CK(lmm::launch_mrg32k3a(2, 12345u, 0, num, mean, std_dev, e->z32.p, e->stream));
+    else
+        LMM_CK(lmm::launch_normals_f32(12345u, 0, numPaths, 40, mean, std_dev, e->z32.as<float>(), e->stream));
     LMM_CK(cudaMemcpyAsync(z, e->z32.p, sizeof(float) * (size_t)num, cudaMemcpyDeviceToHost, e->stream));
     LMM_TRY(run_f32(e, Mode::Fused, e->z32.as<float>(), 0, 0, false, numPaths, nullptr, nullptr,
                     e->out.as<double>(), e->se.as<double>()));
@@ -883,6 +921,36 @@ int lmm_swaption_greeks_f32(float *z, int num, float mean, float std_dev, int se
     *d_v = (float)out[0];
     *d_Lb = (float)out[e->nn];
     return LMM_OK;
+}
+
+// `seed` is accepted and ignored, as in the reference (generateRand uses its
+// default seed 12345).
+int lmm_swaption_greeks(double *z, int num, double mean, double std_dev, int seed, double *d_v,
+                        double *d_Lb, int numPaths)
+{
+    (void)seed;
+    return swaption_greeks_f64(false, z, num, mean, std_dev, d_v, d_Lb, numPaths);
+}
+
+int lmm_swaption_greeks_f32(float *z, int num, float mean, float std_dev, int seed, float *d_v,
+                            float *d_Lb, int numPaths)
+{
+    (void)seed;
+    return swaption_greeks_f32(false, z, num, mean, std_dev, d_v, d_Lb, numPaths);
+}
+
+int lmm_swaption_greeks_mrg32k3a(double *z, int num, double mean, double std_dev, int seed, double *d_v,
+                                 double *d_Lb, int numPaths)
+{
+    (void)seed;
+    return swaption_greeks_f64(true, z, num, mean, std_dev, d_v, d_Lb, numPaths);
+}
+
+int lmm_swaption_greeks_mrg32k3a_f32(float *z, int num, float mean, float std_dev, int seed, float *d_v,
+                                     float *d_Lb, int numPaths)
+{
+    (void)seed;
+    return swaption_greeks_f32(true, z, num, mean, std_dev, d_v, d_Lb, numPaths);
 }
 
 }  // extern "C"

@@ -83,6 +83,14 @@ cudaError_t launch_bump_diff(double *mean, double *se, int nscen, int nout, doub
 // independent FMA chains each; one float per thread to `sink`.
 cudaError_t launch_ffma_peak(int blocks, int iters, float a, float b, float *sink, cudaStream_t s);
 
+// MRG32k3a jump tables (lmm_mrg.cu): A1^(2^k), A2^(2^k) for k < 64 and the
+// per-lane offsets A1^(l*span), A2^(l*span) for l < 32, entries mod m1/m2.
+struct MrgTables {
+    uint32_t p1[64][9], p2[64][9], l1[32][9], l2[32][9];
+};
+// kind 0: uniforms (double), 1: normals (double, PPND16), 2: normals (float, PPND7)
+cudaError_t launch_mrg32k3a(int kind, uint32_t seed, int64_t first, int64_t count, double mean, double sd,
+                            void *out, cudaStream_t s);
 cudaError_t launch_normals_f32(uint64_t seed, int64_t path0, int64_t paths, int nmat, float mean,
                                float sd, float *z, cudaStream_t s);
 cudaError_t launch_normals_f64(uint64_t seed, int64_t path0, int64_t paths, int nmat, double mean,

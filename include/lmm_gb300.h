@@ -165,6 +165,25 @@ int lmm_normals_f32_device(uint64_t seed, int64_t path0, int64_t paths, int32_t 
 int lmm_normals_f64_device(uint64_t seed, int64_t path0, int64_t paths, int32_t nmat,
                            double mean, double std_dev, double *d_z, void *stream);
 
+/* ---- MRG32k3a stream (the reference's generator family) ----------------- */
+/* Replaces generateRand (LiborMarketModel/mklRng.cpp:44-110), which draws
+ * ONE MRG32k3a stream (vslNewStream(..., VSL_BRNG_MRG32K3A, seed), :91),
+ * read sequentially into z with a skip-ahead per thread (:97) and Gaussians
+ * by inversion (VSL_RNG_METHOD_GAUSSIAN_ICDF, :25/:31). These calls write
+ * elements [first, first+count) of that kind of stream: MRG32k3a
+ * (L'Ecuyer 1999) seeded from one 32-bit seed as x = (seed mod m1, 1, 1),
+ * y = (1, 1, 1); u = z/(m1+1) with z in [1, m1]; normals by AS241 (Wichura
+ * 1988): PPND16 in FP64, PPND7 in FP32; out = mean + std_dev * x. MKL's own
+ * seeding, scaling and inversion are not reproduced (closed), so the numbers
+ * are not MKL's. Skip-ahead is exact for any first < 2^63. Enqueued on
+ * `stream` (the current device); count = 0 is a no-op. */
+int lmm_mrg32k3a_uniforms_device(uint32_t seed, int64_t first, int64_t count, double *d_u,
+                                 void *stream);
+int lmm_mrg32k3a_normals_f64_device(uint32_t seed, int64_t first, int64_t count, double mean,
+                                    double std_dev, double *d_z, void *stream);
+int lmm_mrg32k3a_normals_f32_device(uint32_t seed, int64_t first, int64_t count, float mean,
+                                    float std_dev, float *d_z, void *stream);
+
 /* ---- no-allocation variant ---------------------------------------------- */
 /* No counterpart in the reference. Some callers cannot call cudaMalloc: a
  * library embedded in a host application that owns every device allocation
@@ -212,6 +231,13 @@ int lmm_swaption_greeks(double *z, int num, double mean, double std_dev, int see
  * computed with the FP32 adjoint kernels. */
 int lmm_swaption_greeks_f32(float *z, int num, float mean, float std_dev, int seed,
                             float *d_v, float *d_Lb, int numPaths);
+/* The same two calls with z drawn from the MRG32k3a stream above (seed
+ * 12345, elements 0..num-1), the reference's generator family and stream
+ * order, instead of the library's Philox stream. */
+int lmm_swaption_greeks_mrg32k3a(double *z, int num, double mean, double std_dev, int seed,
+                                 double *d_v, double *d_Lb, int numPaths);
+int lmm_swaption_greeks_mrg32k3a_f32(float *z, int num, float mean, float std_dev, int seed,
+                                     float *d_v, float *d_Lb, int numPaths);
 
 #ifdef __cplusplus
 }

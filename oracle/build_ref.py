@@ -1,6 +1,7 @@
 """Build recipe for the oracle libraries (test infrastructure only).
 
-  oracle/_build/liblmm_oracle.so   the FP64 C restatement (oracle/lmm_oracle.c)
+  oracle/_build/liblmm_oracle.so   the FP64 C restatement (oracle/lmm_oracle.c) and
+                                   the MRG32k3a/AS241 stream (oracle/lmm_mrg_oracle.c)
   oracle/_ref/libref_<tag>.so      the UNMODIFIED reference
                                    LiborMarketModel/liborSwaptionGreeks.cpp,
                                    compiled where it lies together with
@@ -49,12 +50,12 @@ def _stale(target, deps):
 
 def build_oracle(force=False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "lmm_oracle.c")
+    srcs = [os.path.join(HERE, "lmm_oracle.c"), os.path.join(HERE, "lmm_mrg_oracle.c")]
     out = os.path.join(BUILD, "liblmm_oracle.so")
-    if force or _stale(out, [src]):
+    if force or _stale(out, srcs):
         tmp = out + f".tmp{os.getpid()}"
         _run(["gcc", "-O3", "-std=c99", "-fopenmp", "-fPIC", "-shared", "-Wall", "-Wextra",
-              "-Wno-unused-parameter", src, "-o", tmp, "-lm"])
+              "-Wno-unused-parameter", *srcs, "-o", tmp, "-lm"])
         os.replace(tmp, out)
     return out
 

@@ -44,6 +44,14 @@ def lib():
         L.lmmo_value.argtypes = [P, dp, C.c_int64, C.c_int32, dp, dp]
         L.lmmo_fd_greeks.argtypes = [P, dp, C.c_int64, C.c_double, C.c_int32, dp]
         L.lmmo_reference_work.argtypes = [P, dp, C.c_int64, C.c_int32, dp, dp]
+        u64p = C.POINTER(C.c_uint64)
+        L.lmmo_mrg32k3a_pow2.argtypes = [C.c_int32, u64p, u64p]
+        L.lmmo_mrg32k3a_uniforms.argtypes = [C.c_uint32, C.c_int64, C.c_int64, dp]
+        L.lmmo_mrg32k3a_normals_f64.argtypes = [C.c_uint32, C.c_int64, C.c_int64, C.c_double,
+                                                C.c_double, dp]
+        L.lmmo_mrg32k3a_normals_f32.argtypes = [C.c_uint32, C.c_int64, C.c_int64, C.c_float,
+                                                C.c_float, fp]
+        L.lmmo_ppnd16_array.argtypes = [dp, C.c_int64, dp]
         for f in ("lmmo_paths", "lmmo_greeks", "lmmo_value", "lmmo_fd_greeks",
                   "lmmo_reference_work", "lmmo_max_threads"):
             getattr(L, f).restype = C.c_int
@@ -83,6 +91,39 @@ def normals_f32(seed, paths, nmat, path0=0):
     z = np.empty(paths * nmat, dtype=np.float32)
     lib().lmmo_normals_f32(seed, path0, paths, nmat, z.ctypes.data_as(C.POINTER(C.c_float)))
     return z
+
+
+def mrg32k3a_pow2(k):
+    """(A1^(2^k) mod m1, A2^(2^k) mod m2) as 3x3 integer lists."""
+    a1 = (C.c_uint64 * 9)()
+    a2 = (C.c_uint64 * 9)()
+    lib().lmmo_mrg32k3a_pow2(k, a1, a2)
+    return [list(a1[3 * i:3 * i + 3]) for i in range(3)], [list(a2[3 * i:3 * i + 3]) for i in range(3)]
+
+
+def mrg32k3a_uniforms(seed, first, count):
+    u = np.empty(count, dtype=np.float64)
+    lib().lmmo_mrg32k3a_uniforms(seed, first, count, _dp(u))
+    return u
+
+
+def mrg32k3a_normals_f64(seed, first, count, mean=0.0, sd=1.0):
+    z = np.empty(count, dtype=np.float64)
+    lib().lmmo_mrg32k3a_normals_f64(seed, first, count, mean, sd, _dp(z))
+    return z
+
+
+def mrg32k3a_normals_f32(seed, first, count, mean=0.0, sd=1.0):
+    z = np.empty(count, dtype=np.float32)
+    lib().lmmo_mrg32k3a_normals_f32(seed, first, count, mean, sd, z.ctypes.data_as(C.POINTER(C.c_float)))
+    return z
+
+
+def ppnd16(p):
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    x = np.empty_like(p)
+    lib().lmmo_ppnd16_array(_dp(p), p.size, _dp(x))
+    return x
 
 
 def _z64(z):
