@@ -35,6 +35,7 @@ EXPORTS = (
     "lmm_swaption_greeks", "lmm_swaption_greeks_f32", "lmm_greeks_f32_device_noalloc",
     "lmm_mrg32k3a_uniforms_device", "lmm_mrg32k3a_normals_f64_device", "lmm_mrg32k3a_normals_f32_device",
     "lmm_swaption_greeks_mrg32k3a", "lmm_swaption_greeks_mrg32k3a_f32",
+    "lmm_engine_set_weights", "lmm_swaption_breakdown_f32_device", "lmm_swaption_breakdown_f64_device",
 )
 
 
@@ -101,6 +102,9 @@ def lib():
         "lmm_swaption_greeks": ([dp, C.c_int, C.c_double, C.c_double, C.c_int, dp, dp, C.c_int], C.c_int),
         "lmm_swaption_greeks_f32": ([fp, C.c_int, C.c_float, C.c_float, C.c_int, fp, fp, C.c_int], C.c_int),
         "lmm_greeks_f32_device_noalloc": ([P, vp, i64, vp, vp, vp], C.c_int),
+        "lmm_engine_set_weights": ([vp, dp], C.c_int),
+        "lmm_swaption_breakdown_f32_device": ([vp, vp, i64, vp, vp], C.c_int),
+        "lmm_swaption_breakdown_f64_device": ([vp, vp, i64, vp, vp], C.c_int),
         "lmm_mrg32k3a_uniforms_device": ([C.c_uint32, i64, i64, vp, vp], C.c_int),
         "lmm_mrg32k3a_normals_f64_device": ([C.c_uint32, i64, i64, C.c_double, C.c_double, vp, vp], C.c_int),
         "lmm_mrg32k3a_normals_f32_device": ([C.c_uint32, i64, i64, C.c_float, C.c_float, vp, vp], C.c_int),
@@ -163,6 +167,7 @@ class Engine:
         self.cfg = cfg
         self._ref = _ParamsRef(cfg)
         self.nn, self.nmat, self.nscen = int(cfg.nn), int(cfg.nmat), int(self._ref.L0.shape[0])
+        self.nopt = int(len(cfg.swaprates))
         self.nout = 1 + 2 * self.nn
         h = C.c_void_p()
         _check(lib().lmm_engine_create(C.byref(self._ref.p), device, C.byref(h)), "lmm_engine_create")
@@ -249,6 +254,26 @@ class Engine:
     def bump_greeks_f64_device(self, d_z: int, paths: int, h: float, d_out: int, d_se: int = 0):
         _check(lib().lmm_bump_greeks_f64_device(self.h, d_z, paths, h, d_out, d_se or None),
                "lmm_bump_greeks_f64_device")
+
+    # portfolio weights and per-swaption breakdown
+    def set_weights(self, weights=None):
+        """Notional weight per swaption (order of the config's swaprates); None = all 1."""
+        if weights is None:
+            _check(lib().lmm_engine_set_weights(self.h, None), "lmm_engine_set_weights")
+            return
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if w.shape != (self.nopt,):
+            raise LmmError(-1, "set_weights", f"need {self.nopt} weights")
+        _check(lib().lmm_engine_set_weights(self.h, _dp(w)), "lmm_engine_set_weights")
+
+    def breakdown_f32_device(self, d_z: int, paths: int, d_out: int, d_se: int = 0):
+        """[nopt][nscen][1+2nn]: each swaption's value and Greeks at unit weight."""
+        _check(lib().lmm_swaption_breakdown_f32_device(self.h, d_z, paths, d_out, d_se or None),
+               "lmm_swaption_breakdown_f32_device")
+
+    def breakdown_f64_device(self, d_z: int, paths: int, d_out: int, d_se: int = 0):
+        _check(lib().lmm_swaption_breakdown_f64_device(self.h, d_z, paths, d_out, d_se or None),
+               "lmm_swaption_breakdown_f64_device")
 
     # forward/backward pair
     def tape(self, paths: int) -> "Tape":

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -95,6 +96,9 @@ struct lmm_engine {
     int sms = 0;
     DevModel dm{};
     DevBuf model;                  // all model arrays
+    std::vector<int> opt_slot;     // opt_slot[o]: grouped position of swaption o
+    float *wf_rows = nullptr;      // [1+nopt][nopt] weights: row 0 the caller's, row 1+g unit at g
+    double *wd_rows = nullptr;
     DevBuf partial, z32, z64, out, se, flag, vbar;
     std::map<int, int> bps;        // cached blocks per SM per kernel variant
     int32_t last_launches = 0;
@@ -446,6 +450,18 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
     const size_t o_l0d = sect(sizeof(double) * L0f.size()), o_lamd = sect(sizeof(double) * nn);
     const size_t o_ost = sect(sizeof(int) * (M + 1)), o_okf = sect(sizeof(float) * std::max(1, nopt));
     const size_t o_okd = sect(sizeof(double) * std::max(1, nopt));
+    const size_t wrow = (size_t)std::max(1, nopt);
+    const size_t o_wf = sect(sizeof(float) * wrow * (nopt + 1)), o_wd = sect(sizeof(double) * wrow * (nopt + 1));
+    std::vector<float> wf(wrow * (nopt + 1), 0.0f);
+    std::vector<double> wd(wrow * (nopt + 1), 0.0);
+    for (int g = 0; g < nopt; ++g) {
+        wf[g] = 1.0f;
+        wd[g] = 1.0;
+        wf[wrow * (1 + g) + g] = 1.0f;
+        wd[wrow * (1 + g) + g] = 1.0;
+    }
+    e->opt_slot.assign(nopt, 0);
+    for (int g = 0; g < nopt; ++g) e->opt_slot[order[g]] = g;
     LMM_TRY(e->model.ensure(off));
     char *base = e->model.as<char>();
     auto up = [&](size_t o, const void *src, size_t bytes) {
@@ -460,6 +476,10 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
     LMM_CK(up(o_ost, ost.data(), sizeof(int) * (M + 1)));
     LMM_CK(up(o_okf, okf.data(), sizeof(float) * nopt));
     LMM_CK(up(o_okd, okd.data(), sizeof(double) * nopt));
+    LMM_CK(up(o_wf, wf.data(), sizeof(float) * wf.size()));
+    LMM_CK(up(o_wd, wd.data(), sizeof(double) * wd.size()));
+    e->wf_rows = reinterpret_cast<float *>(base + o_wf);
+    e->wd_rows = reinterpret_cast<double *>(base + o_wd);
 
     DevModel &m = e->dm;
     m.nn = nn;
@@ -480,6 +500,8 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
     m.opt_start = reinterpret_cast<const int *>(base + o_ost);
     m.optKf = reinterpret_cast<const float *>(base + o_okf);
     m.optKd = reinterpret_cast<const double *>(base + o_okd);
+    m.optWf = e->wf_rows;
+    m.optWd = e->wd_rows;
 
     LMM_CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
     e->own_stream = true;
@@ -611,6 +633,70 @@ int lmm_greeks_f32_device(lmm_engine *e, const float *d_z, int64_t paths, double
 {
     if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
     return run_f32(e, Mode::Fused, d_z, 0, 0, false, paths, nullptr, nullptr, d_out, d_se);
+}
+
+// ---- portfolio weights and per-swaption breakdown ---------------------------
+
+int lmm_engine_set_weights(lmm_engine *e, const double *weights)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    const int nopt = e->nopt;
+    std::vector<double> wd(std::max(1, nopt), 1.0);
+    std::vector<float> wf(std::max(1, nopt), 1.0f);
+    for (int o = 0; o < nopt && weights; ++o) {
+        if (!std::isfinite(weights[o])) return fail(LMM_ERR_INVALID_ARG, "weights must be finite");
+        wd[e->opt_slot[o]] = weights[o];
+        wf[e->opt_slot[o]] = (float)weights[o];
+    }
+    LMM_TRY(set_device(e));
+    // ordered after earlier work on the engine's stream; the host vectors
+    // stay alive until the copies have run
+    LMM_CK(cudaMemcpyAsync(e->wd_rows, wd.data(), sizeof(double) * nopt, cudaMemcpyHostToDevice, e->stream));
+    LMM_CK(cudaMemcpyAsync(e->wf_rows, wf.data(), sizeof(float) * nopt, cudaMemcpyHostToDevice, e->stream));
+    LMM_CK(cudaStreamSynchronize(e->stream));
+    return LMM_OK;
+}
+
+// One fused call per swaption with that swaption alone at unit weight: the
+// model is passed to each launch by value, so only the weight pointers change.
+static int per_swaption(lmm_engine *e, const std::function<int(int)> &call)
+{
+    const DevModel saved = e->dm;
+    const size_t row = (size_t)std::max(1, e->nopt);
+    int rc = LMM_OK;
+    int32_t launches = 0;
+    for (int o = 0; o < e->nopt && rc == LMM_OK; ++o) {
+        e->dm.optWf = e->wf_rows + row * (1 + e->opt_slot[o]);
+        e->dm.optWd = e->wd_rows + row * (1 + e->opt_slot[o]);
+        rc = call(o);
+        launches += e->last_launches;
+    }
+    e->dm = saved;
+    e->last_launches = launches;
+    return rc;
+}
+
+int lmm_swaption_breakdown_f32_device(lmm_engine *e, const float *d_z, int64_t paths, double *d_out,
+                                      double *d_se)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    if (e->nopt < 1) return fail(LMM_ERR_INVALID_ARG, "the portfolio has no swaptions");
+    const size_t per = (size_t)e->nscen * (1 + 2 * e->nn);
+    return per_swaption(e, [&](int o) {
+        return run_f32(e, Mode::Fused, d_z, 0, 0, false, paths, nullptr, nullptr, d_out + per * o,
+                       d_se ? d_se + per * o : nullptr);
+    });
+}
+
+int lmm_swaption_breakdown_f64_device(lmm_engine *e, const double *d_z, int64_t paths, double *d_out,
+                                      double *d_se)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    if (e->nopt < 1) return fail(LMM_ERR_INVALID_ARG, "the portfolio has no swaptions");
+    const size_t per = (size_t)e->nscen * (1 + 2 * e->nn);
+    return per_swaption(e, [&](int o) {
+        return run_f64(e, d_z, paths, d_out + per * o, d_se ? d_se + per * o : nullptr);
+    });
 }
 
 // Host call with the copy overlapped: the normals go up in kHostChunks

@@ -113,7 +113,9 @@ struct TppLayout {
     static constexpr int ost = il0 + 4 * NN;                         // int[M+1]
     static constexpr int okf = align16(ost + 4 * (M + 1));           // float[kMaxNopt]
     static constexpr int okd = align16(okf + 4 * kMaxNopt);          // double[kMaxNopt]
-    static constexpr int vt = align16(okd + 8 * kMaxNopt);           // float[NMAT][B]
+    static constexpr int owf = align16(okd + 8 * kMaxNopt);          // float[kMaxNopt] weights
+    static constexpr int owd = align16(owf + 4 * kMaxNopt);          // double[kMaxNopt]
+    static constexpr int vt = align16(owd + 8 * kMaxNopt);           // float[NMAT][B]
     static constexpr int vt_bytes = MODE == Mode::Fused ? 4 * NMAT * B : 0;
     static constexpr int vg = vt + vt_bytes;                         // float[PAD+NN][B]
     static constexpr int vg_bytes = MODE == Mode::Forward ? 0 : 4 * (PAD + NN) * B;
@@ -220,8 +222,8 @@ __device__ __forceinline__ void rev_group(float (&L)[NN], float (&Pb)[NN], RevSt
 // :139 rounded to FP32, for the adjoint.
 template <int NN, int NMAT, int B>
 __device__ __forceinline__ double payoff_forward(const float (&L)[NN], float delta, const int *ost,
-                                                 const double *oKd, double *disc_out, float *Bst,
-                                                 unsigned long long *mask_out)
+                                                 const double *oKd, const double *oWd, double *disc_out,
+                                                 float *Bst, unsigned long long *mask_out)
 {
     constexpr int M = NN - NMAT;
     double disc = 1.0;
@@ -239,7 +241,7 @@ __device__ __forceinline__ double payoff_forward(const float (&L)[NN], float del
         for (int o = ost[m]; o < o1; ++o) {
             const double sw = fma(oKd[o], s, b) - 1.0;
             if (sw < 0.0) {
-                vs -= 100.0 * sw;
+                vs -= (100.0 * sw) * oWd[o];
                 mask |= 1ull << o;
             }
         }
@@ -258,7 +260,7 @@ template <int NN, int NMAT, int B>
 __device__ __forceinline__ void payoff_adjoint(const float (&L)[NN], float (&Pb)[NN], float vbar,
                                                double V, double disc, const float *Bst,
                                                unsigned long long mask, float delta,
-                                               const int *ost, const float *oKf)
+                                               const int *ost, const float *oKf, const float *oWf)
 {
     constexpr int M = NN - NMAT;
     const float scale = -vbar * (float)disc * delta;
@@ -271,8 +273,8 @@ __device__ __forceinline__ void payoff_adjoint(const float (&L)[NN], float (&Pb)
         const int o1 = ost[m + 1];
         for (int o = ost[m]; o < o1; ++o) {
             if ((mask >> o) & 1ull) {
-                Sb -= 100.0f * oKf[o];
-                Bb -= 100.0f;
+                Sb -= (100.0f * oKf[o]) * oWf[o];
+                Bb -= 100.0f * oWf[o];
             }
         }
         Bb = fmaf(delta, Sb, Bb);
@@ -580,6 +582,8 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
     float *okf_s = reinterpret_cast<float *>(smem + Lay::okf);
     double *okd_s = reinterpret_cast<double *>(smem + Lay::okd);
+    float *owf_s = reinterpret_cast<float *>(smem + Lay::owf);
+    double *owd_s = reinterpret_cast<double *>(smem + Lay::owd);
     float *vt_s = reinterpret_cast<float *>(smem + Lay::vt);
     float *vg_s = reinterpret_cast<float *>(smem + Lay::vg);
     double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
@@ -599,6 +603,8 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     for (int i = tid; i < m.nopt; i += B) {
         okf_s[i] = m.optKf[i];
         okd_s[i] = m.optKd[i];
+        owf_s[i] = m.optWf[i];
+        owd_s[i] = m.optWd[i];
     }
     double *acc = acc_s + warp * 2 * NOUT;
     for (int i = tid; i < Lay::NW * 2 * NOUT; i += B) acc_s[i] = 0.0;
@@ -646,10 +652,10 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         unsigned long long mask = 0ull;
         // B[m] goes to this thread's vega column, unused until the reverse sweep.
         float *Bst = MODE == Mode::Forward ? nullptr : vg0;
-        const double V = payoff_forward<NN, NMAT, B>(L, delta, ost_s, okd_s, &disc, Bst, &mask);
+        const double V = payoff_forward<NN, NMAT, B>(L, delta, ost_s, okd_s, owd_s, &disc, Bst, &mask);
 
         if (MODE != Mode::Forward) {
-            payoff_adjoint<NN, NMAT, B>(L, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s);
+            payoff_adjoint<NN, NMAT, B>(L, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s, owf_s);
 #pragma unroll
             for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
             zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);

@@ -32,7 +32,7 @@ __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(
 // Shared-memory layout (bytes), shared by host and device.
 struct WppLay {
     int nn, nmat, S, nck, nout, M;
-    size_t kc, kd, l0, il0, ost, okf, okd, warp0, per_warp, ck, vg, lw, bw, acc, bytes;
+    size_t kc, kd, l0, il0, ost, okf, okd, owf, owd, warp0, per_warp, ck, vg, lw, bw, acc, bytes;
 };
 
 __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
@@ -52,6 +52,8 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
     L.ost = o; o = al16(o + 4 * (size_t)(L.M + 1));
     L.okf = o; o = al16(o + 4 * (size_t)kMaxNopt);
     L.okd = o; o = al16(o + 8 * (size_t)kMaxNopt);
+    L.owf = o; o = al16(o + 4 * (size_t)kMaxNopt);    // notional weights
+    L.owd = o; o = al16(o + 8 * (size_t)kMaxNopt);
     L.warp0 = o;
     size_t w = 0;
     L.ck = w; w = al16(w + 4 * (size_t)L.nck * 32 * S);   // checkpoints [nck][32*S]
@@ -213,6 +215,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     int *ost_s = reinterpret_cast<int *>(smem + Ly.ost);
     float *okf_s = reinterpret_cast<float *>(smem + Ly.okf);
     double *okd_s = reinterpret_cast<double *>(smem + Ly.okd);
+    float *owf_s = reinterpret_cast<float *>(smem + Ly.owf);
+    double *owd_s = reinterpret_cast<double *>(smem + Ly.owd);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned char *wbase = smem + Ly.warp0 + warp * Ly.per_warp;
     float *ck_s = reinterpret_cast<float *>(wbase + Ly.ck);
@@ -232,6 +236,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     for (int i = tid; i < m.nopt; i += kWppBlock) {
         okf_s[i] = m.optKf[i];
         okd_s[i] = m.optKd[i];
+        owf_s[i] = m.optWf[i];
+        owd_s[i] = m.optWd[i];
     }
     for (int i = lane; i < 2 * nout; i += 32) acc[i] = 0.0;
     for (int i = lane; i < 32 * S; i += 32) vg_s[i] = 0.0f;
@@ -284,7 +290,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
                     const double sw = fma(okd_s[o], ss, bb) - 1.0;
                     if (sw < 0.0) {
-                        vs -= 100.0 * sw;
+                        vs -= (100.0 * sw) * owd_s[o];
                         mask |= 1ull << o;
                     }
                 }
@@ -302,8 +308,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 const float Bm = bw_s[mm];
                 for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
                     if ((mask >> o) & 1ull) {
-                        Sb -= 100.0f * okf_s[o];
-                        Bb -= 100.0f;
+                        Sb -= (100.0f * okf_s[o]) * owf_s[o];
+                        Bb -= 100.0f * owf_s[o];
                     }
                 }
                 Bb = fmaf(delta, Sb, Bb);

@@ -26,7 +26,7 @@ struct F64Smem {
 // portfolio_b :133-171 and :186-197 in FP64; returns the discounted value.
 // Bst (if given) receives the annuity factors B[m] of :139 for the adjoint.
 __device__ double payoff_value_f64(const double *L, int nn, int nmat, double d, const int *ost,
-                                   const double *okd, double *disc_out, double *Bst,
+                                   const double *okd, const double *okw, double *disc_out, double *Bst,
                                    unsigned long long *mask_out)
 {
     double b = 1.0, s = 0.0, vs = 0.0;
@@ -38,7 +38,7 @@ __device__ double payoff_value_f64(const double *L, int nn, int nmat, double d, 
         for (int o = ost[m]; o < ost[m + 1]; ++o) {
             const double sw = b + okd[o] * s - 1.0;
             if (sw < 0.0) {
-                vs += -100.0 * sw;
+                vs += (-100.0 * sw) * okw[o];
                 mask |= 1ull << o;
             }
         }
@@ -74,13 +74,17 @@ k_f64_greeks(const DevModel m, const double *__restrict__ z, const Work w)
     const int NW = kF64Block / 32;
     double *lam_s = reinterpret_cast<double *>(smem);
     double *okd_s = lam_s + kMaxNN;
-    double *acc_s = okd_s + kMaxNopt;
+    double *okw_s = okd_s + kMaxNopt;
+    double *acc_s = okw_s + kMaxNopt;
     int *ost_s = reinterpret_cast<int *>(acc_s + NW * 2 * nout);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int scen = blockIdx.x / w.items, item = blockIdx.x % w.items;
     for (int i = tid; i < nn; i += kF64Block) lam_s[i] = m.lamd[i];
     for (int i = tid; i <= M; i += kF64Block) ost_s[i] = m.opt_start[i];
-    for (int i = tid; i < m.nopt; i += kF64Block) okd_s[i] = m.optKd[i];
+    for (int i = tid; i < m.nopt; i += kF64Block) {
+        okd_s[i] = m.optKd[i];
+        okw_s[i] = m.optWd[i];
+    }
     for (int i = tid; i < NW * 2 * nout; i += kF64Block) acc_s[i] = 0.0;
     __syncthreads();
     double *acc = acc_s + warp * 2 * nout;
@@ -101,7 +105,7 @@ k_f64_greeks(const DevModel m, const double *__restrict__ z, const Work w)
         forward_f64(L, Vt, zp, lam_s, nn, nmat, d, sqd);
         double disc;
         unsigned long long mask;
-        const double V = payoff_value_f64(L, nn, nmat, d, ost_s, okd_s, &disc, Bs, &mask);
+        const double V = payoff_value_f64(L, nn, nmat, d, ost_s, okd_s, okw_s, &disc, Bs, &mask);
         // payoff adjoint (:173-184 with the rate kept apart from its adjoint,
         // then :199-209), written as log-adjoints Pb = L * dV/dL. B[m] comes
         // from the forward as in the reference: rebuilding it backwards from
@@ -113,8 +117,8 @@ k_f64_greeks(const DevModel m, const double *__restrict__ z, const Work w)
                 const double Ln = L[nmat + mm];
                 for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
                     if ((mask >> o) & 1ull) {
-                        Sb += -100.0 * okd_s[o];
-                        Bb += -100.0;
+                        Sb += (-100.0 * okd_s[o]) * okw_s[o];
+                        Bb += -100.0 * okw_s[o];
                     }
                 }
                 Bb += d * Sb;
@@ -175,7 +179,8 @@ k_f64_bump(const DevModel m, const double *__restrict__ z, double h, const Work 
     const int NW = kF64Block / 32;
     double *lam_s = reinterpret_cast<double *>(smem);
     double *okd_s = lam_s + kMaxNN;
-    double *acc_s = okd_s + kMaxNopt;
+    double *okw_s = okd_s + kMaxNopt;
+    double *acc_s = okw_s + kMaxNopt;
     int *ost_s = reinterpret_cast<int *>(acc_s + NW * 2);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb = 1 + 2 * nn;
@@ -184,7 +189,10 @@ k_f64_bump(const DevModel m, const double *__restrict__ z, double h, const Work 
     for (int i = tid; i < nn; i += kF64Block)
         lam_s[i] = m.lamd[i] + ((var > nn && i == var - nn - 1) ? h : 0.0);
     for (int i = tid; i <= M; i += kF64Block) ost_s[i] = m.opt_start[i];
-    for (int i = tid; i < m.nopt; i += kF64Block) okd_s[i] = m.optKd[i];
+    for (int i = tid; i < m.nopt; i += kF64Block) {
+        okd_s[i] = m.optKd[i];
+        okw_s[i] = m.optWd[i];
+    }
     if (tid < NW * 2) acc_s[tid] = 0.0;
     __syncthreads();
     const double d = m.deltad, sqd = m.sqdd;
@@ -200,7 +208,7 @@ k_f64_bump(const DevModel m, const double *__restrict__ z, double h, const Work 
         forward_f64(L, nullptr, zp, lam_s, nn, nmat, d, sqd);
         double disc;
         unsigned long long mask;
-        double V = payoff_value_f64(L, nn, nmat, d, ost_s, okd_s, &disc, nullptr, &mask);
+        double V = payoff_value_f64(L, nn, nmat, d, ost_s, okd_s, okw_s, &disc, nullptr, &mask);
         V = active ? V : 0.0;
         const double s1 = warp_sum(V), s2 = warp_sum(V * V);
         if (lane == 0) {
@@ -218,7 +226,7 @@ k_f64_bump(const DevModel m, const double *__restrict__ z, double h, const Work 
 
 size_t f64_smem_bytes(int nout)
 {
-    return sizeof(double) * (kMaxNN + kMaxNopt + (kF64Block / 32) * 2 * (size_t)nout) +
+    return sizeof(double) * (kMaxNN + 2 * kMaxNopt + (kF64Block / 32) * 2 * (size_t)nout) +
            sizeof(int) * (kMaxNN + 1);
 }
 

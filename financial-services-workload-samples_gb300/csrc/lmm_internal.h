@@ -30,6 +30,8 @@ struct DevModel {
     const int *opt_start;                 // [nn-nmat+1] options grouped by maturity-1 (CSR)
     const float *optKf;                   // [nopt] strikes in that grouped order
     const double *optKd;                  // [nopt]
+    const float *optWf;                   // [nopt] notional weights in that grouped order
+    const double *optWd;                  // [nopt] (the reference's portfolio: all 1)
 };
 
 // Path partition of one launch: grid = nscen * items blocks; block b takes

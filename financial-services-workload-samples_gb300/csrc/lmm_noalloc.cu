@@ -42,6 +42,8 @@ struct NoallocModel {
     int ost[kM + 1];
     float okf[LMM_MAX_NOPT];
     double okd[LMM_MAX_NOPT];
+    float owf[LMM_MAX_NOPT];     // notional weights: the reference's portfolio, all 1
+    double owd[LMM_MAX_NOPT];
 };
 
 constexpr size_t kModelBytes = (sizeof(NoallocModel) + 255) & ~size_t(255);
@@ -124,6 +126,8 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
         const int slot = fill[p->maturities[o] - 1]++;
         hm.okf[slot] = (float)p->swaprates[o];
         hm.okd[slot] = p->swaprates[o];
+        hm.owf[slot] = 1.0f;
+        hm.owd[slot] = 1.0;
     }
 
     unsigned char *base = ds.scratch;
@@ -151,6 +155,8 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
     m.opt_start = dmod->ost;
     m.optKf = dmod->okf;
     m.optKd = dmod->okd;
+    m.optWf = dmod->owf;
+    m.optWd = dmod->owd;
 
     // About two waves of the device, capped by the partial-sum space.
     const int64_t block = lmm::tpp_block_threads();

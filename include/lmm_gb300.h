@@ -156,6 +156,24 @@ int lmm_bump_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, 
 int lmm_bump_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double h,
                              double *out, double *se);
 
+/* ---- portfolio weights and per-swaption breakdown ----------------------- */
+/* The reference prices a fixed portfolio: every swaption with notional 100
+ * (portfolio_b, liborSwaptionGreeks.cpp:159-171). weights[o] (one per
+ * swaption, in the order of lmm_params.swaprates) scales swaption o's payoff
+ * in every later call of the engine -- value and all Greeks, FP32 and FP64,
+ * the forward/backward pair and the bump comparator; NULL restores all 1.
+ * Weights must be finite (0 and negative values are allowed: a short
+ * position). Waits for the engine's earlier work. */
+int lmm_engine_set_weights(lmm_engine *e, const double *weights);
+/* Per-swaption breakdown: for each swaption o, the value and all 2*nn Greeks
+ * of that swaption alone at unit weight (times the reference's 100), as one
+ * fused call each. d_out/d_se: [nopt][nscen][1+2*nn] (swaption-major; d_se
+ * may be NULL). Summing over o gives the unit-weight portfolio. */
+int lmm_swaption_breakdown_f32_device(lmm_engine *e, const float *d_z, int64_t paths,
+                                      double *d_out, double *d_se);
+int lmm_swaption_breakdown_f64_device(lmm_engine *e, const double *d_z, int64_t paths,
+                                      double *d_out, double *d_se);
+
 /* ---- normals ---------------------------------------------------------- */
 /* z[p*nmat+n] for paths path0..path0+paths-1, the same numbers the Philox
  * mode consumes in-kernel (FP32 spec). Enqueued on `stream`. */

@@ -53,6 +53,8 @@ typedef struct {
     const double *lambda;/* [nn] vol by time to maturity, read as lambda[i-n-1] (:65,:102) */
     const int32_t *maturities; /* [nopt] swap length in periods (params.h:38) */
     const double *swaprates;   /* [nopt] strikes                (params.h:39) */
+    const double *weights;     /* [nopt] notional weight of each swaption (the
+                                  reference's portfolio: all 1); NULL = all 1 */
 } lmmo_params;
 
 /* ------------------------------------------------------------------ */
@@ -239,12 +241,13 @@ static void blk_payoff(const lmmo_params *p, blk_work *w, double *L, double *v, 
     for (int o = 0; o < p->nopt; ++o) {
         const int m = p->maturities[o] - 1;
         const double K = p->swaprates[o];
+        const double wo = p->weights ? p->weights[o] : 1.0;
         for (int j = 0; j < BLK; ++j) {
             double swapval = w->B[m * BLK + j] + K * w->S[m * BLK + j] - 1.0;
             if (swapval < 0.0) {
-                v[j] += -100.0 * swapval;
-                w->Sb[m * BLK + j] += -100.0 * K;
-                w->Bb[m * BLK + j] += -100.0;
+                v[j] += (-100.0 * swapval) * wo;
+                w->Sb[m * BLK + j] += (-100.0 * K) * wo;
+                w->Bb[m * BLK + j] += -100.0 * wo;
             }
         }
     }

@@ -20,7 +20,8 @@ class OracleParams(C.Structure):
     _fields_ = [("nn", C.c_int32), ("nmat", C.c_int32), ("nopt", C.c_int32),
                 ("reserved", C.c_int32), ("delta", C.c_double),
                 ("L0", C.POINTER(C.c_double)), ("lam", C.POINTER(C.c_double)),
-                ("maturities", C.POINTER(C.c_int32)), ("swaprates", C.POINTER(C.c_double))]
+                ("maturities", C.POINTER(C.c_int32)), ("swaprates", C.POINTER(C.c_double)),
+                ("weights", C.POINTER(C.c_double))]
 
 
 def _dp(a):
@@ -62,15 +63,18 @@ def lib():
 class _Bound:
     """Keeps the numpy arrays a params struct points into alive."""
 
-    def __init__(self, cfg, L0=None, lam=None):
+    def __init__(self, cfg, L0=None, lam=None, weights=None):
         self.L0 = np.ascontiguousarray(cfg.L0 if L0 is None else L0, dtype=np.float64)
         self.lam = np.ascontiguousarray(cfg.lam if lam is None else lam, dtype=np.float64)
         assert self.L0.ndim == 1, "the oracle takes one curve; loop over scenarios"
         self.mat = np.ascontiguousarray(cfg.maturities, dtype=np.int32)
         self.rates = np.ascontiguousarray(cfg.swaprates, dtype=np.float64)
+        self.w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        assert self.w is None or self.w.shape == self.rates.shape
         self.p = OracleParams(cfg.nn, cfg.nmat, int(self.mat.shape[0]), 0, float(cfg.delta),
                               _dp(self.L0), _dp(self.lam),
-                              self.mat.ctypes.data_as(C.POINTER(C.c_int32)), _dp(self.rates))
+                              self.mat.ctypes.data_as(C.POINTER(C.c_int32)), _dp(self.rates),
+                              _dp(self.w) if self.w is not None else None)
 
 
 def philox4x32_10(ctr, key):
@@ -130,9 +134,10 @@ def _z64(z):
     return np.ascontiguousarray(z, dtype=np.float64)
 
 
-def greeks(cfg, z, paths=None, aliased=False, threads=0, L0=None, lam=None):
-    """(mean[1+2nn], se[1+2nn]): value, dV/dL0[i], dV/dlambda[k]."""
-    b = _Bound(cfg, L0, lam)
+def greeks(cfg, z, paths=None, aliased=False, threads=0, L0=None, lam=None, weights=None):
+    """(mean[1+2nn], se[1+2nn]): value, dV/dL0[i], dV/dlambda[k]; `weights`
+    scales each swaption's payoff (default all 1, the reference's portfolio)."""
+    b = _Bound(cfg, L0, lam, weights)
     z = _z64(z)
     paths = cfg.paths if paths is None else paths
     m = np.zeros(cfg.nout)
