@@ -345,6 +345,25 @@ def run_ours(args):
                              path0=rank_path0(rank, n))
         torch.cuda.synchronize(dev)
 
+    # ---- per-swaption breakdown (value + all Greeks of each swaption alone) --
+    breakdown = None
+    if rank == 0 and not args.skip_breakdown:
+        nopt = len(cfg.swaprates)
+        bo = torch.zeros(nopt * nout, dtype=torch.float64, device=dev)
+        eng.breakdown_f32_device(dz.data_ptr(), n, bo.data_ptr())
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b0.record(stream)
+        eng.breakdown_f32_device(dz.data_ptr(), n, bo.data_ptr())
+        b1.record(stream)
+        torch.cuda.synchronize(dev)
+        bms = b0.elapsed_time(b1)
+        bsum = bo.view(nopt, nout).sum(0).cpu().numpy()
+        scale = np.abs(res32).max()
+        breakdown = {"swaptions": nopt, "ms": bms, "launches": eng.last_launches,
+                     "paths_per_s_per_swaption": nopt * n / (bms * 1e-3),
+                     "max_abs_diff_sum_vs_portfolio_over_scale": float(np.max(np.abs(bsum - res32)) / scale)}
+        del bo
+
     # ---- FP64 bump-and-revalue comparator on a bounded sample -------------
     bump = None
     if rank == 0 and not args.skip_bump:
@@ -421,7 +440,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": 2 * 8 * nout + 4, "launches_per_step": e2e_launches,
                     "api": "lmm_greeks_f32_host (pinned host normals)"},
             "roofline": roof, "clocks": clk.summary(), "accuracy": acc, "phase_split": phases,
-            "rng_mrg32k3a": rng,
+            "rng_mrg32k3a": rng, "swaption_breakdown": breakdown,
             "fp64_bump_comparator": bump,
             "other_workloads": others}
     if rank == 0 and not args.skip_cpu:
@@ -452,6 +471,7 @@ def main():
     ap.add_argument("--skip-others", action="store_true")
     ap.add_argument("--skip-phases", action="store_true")
     ap.add_argument("--skip-rng", action="store_true")
+    ap.add_argument("--skip-breakdown", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
