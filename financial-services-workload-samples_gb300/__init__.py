@@ -36,6 +36,7 @@ EXPORTS = (
     "lmm_mrg32k3a_uniforms_device", "lmm_mrg32k3a_normals_f64_device", "lmm_mrg32k3a_normals_f32_device",
     "lmm_swaption_greeks_mrg32k3a", "lmm_swaption_greeks_mrg32k3a_f32",
     "lmm_engine_set_weights", "lmm_swaption_breakdown_f32_device", "lmm_swaption_breakdown_f64_device",
+    "lmm_mufu_peak_gops",
 )
 
 
@@ -85,6 +86,7 @@ def lib():
         "lmm_engine_set_timing": ([vp, i32], C.c_int),
         "lmm_engine_kernel_time": ([vp, dp, dp], C.c_int),
         "lmm_fp32_peak_tflops": ([i32, C.c_double, dp], C.c_int),
+        "lmm_mufu_peak_gops": ([i32, C.c_double, dp, dp, dp], C.c_int),
         "lmm_greeks_f32_host": ([vp, fp, i64, dp, dp], C.c_int),
         "lmm_greeks_f32_device": ([vp, vp, i64, vp, vp], C.c_int),
         "lmm_greeks_philox_host": ([vp, u64, i64, i64, dp, dp], C.c_int),
@@ -313,6 +315,13 @@ def fp32_peak_tflops(device: int = 0, ms: float = 200.0) -> float:
     t = C.c_double()
     _check(lib().lmm_fp32_peak_tflops(device, ms, C.byref(t)), "lmm_fp32_peak_tflops")
     return t.value
+
+
+def mufu_peak_gops(device: int = 0, ms: float = 100.0) -> dict:
+    """Measured MUFU throughput (10^9 ops/s): ex2, rcp and the two alternating."""
+    a, b, c = C.c_double(), C.c_double(), C.c_double()
+    _check(lib().lmm_mufu_peak_gops(device, ms, C.byref(a), C.byref(b), C.byref(c)), "lmm_mufu_peak_gops")
+    return {"ex2": a.value, "rcp": b.value, "mixed": c.value}
 
 
 def normals_f32_device(seed: int, paths: int, nmat: int, d_z: int, stream: int = 0, path0: int = 0):

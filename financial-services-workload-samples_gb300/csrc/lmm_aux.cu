@@ -118,6 +118,31 @@ __global__ void __launch_bounds__(256) k_ffma_peak(int iters, float a, float b, 
     sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// MUFU throughput probe: 16 independent chains per thread of ex2 (KIND 0:
+// x = 2^-x, which stays in (1/2, 1)), rcp (KIND 1: x = 1/(1+x), which tends
+// to 0.618; x = 1/x would be folded away) or both alternately (KIND 2), so
+// the special-function pipe, not latency, limits.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_mufu_peak(int iters, float *sink)
+{
+    float x[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) x[j] = 0.5f + (float)(threadIdx.x + j) * 1e-6f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (KIND == 0 || (KIND == 2 && (j & 1) == 0))
+                x[j] = ex2_approx(-x[j]);
+            else
+                x[j] = rcp_approx(x[j] + 1.0f);
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) s += x[j];
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 unsigned grid_for(int64_t work, int block)
 {
     int64_t g = (work + block - 1) / block;
@@ -147,6 +172,17 @@ cudaError_t launch_bump_diff(double *mean, double *se, int nscen, int nout, doub
 cudaError_t launch_ffma_peak(int blocks, int iters, float a, float b, float *sink, cudaStream_t s)
 {
     k_ffma_peak<<<blocks, 256, 0, s>>>(iters, a, b, sink);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mufu_peak(int kind, int blocks, int iters, float *sink, cudaStream_t s)
+{
+    switch (kind) {
+        case 0: k_mufu_peak<0><<<blocks, 256, 0, s>>>(iters, sink); break;
+        case 1: k_mufu_peak<1><<<blocks, 256, 0, s>>>(iters, sink); break;
+        case 2: k_mufu_peak<2><<<blocks, 256, 0, s>>>(iters, sink); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

@@ -193,16 +193,38 @@ int blocks_per_sm(lmm_engine *e, int family, Mode mode, bool philox, int *out)
     return LMM_OK;
 }
 
-// Splits `paths` per virtual scenario into items so that the grid is about
-// `waves` full waves of the device, and sizes the partial-sum scratch.
-int plan(lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int nout, Work *w,
-         int waves = 2)
+// Items per virtual scenario (and paths per thread) of a launch. Each block
+// runs ppt batches of paths, all blocks equally long, so a launch costs
+// ceil(blocks / slots) block-times, slots = SMs x resident blocks per SM.
+// The plan takes the fewest waves (1..8) whose blocks fill at least 97% of
+// the slots they occupy: one wave for one scenario (every block starts at
+// once, no staggered tail), three waves for 256 scenarios (256 x 7 blocks
+// of 608 slots) where one wave would leave a quarter-full second wave.
+void plan_items(const lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int64_t *items,
+                int64_t *ppt)
 {
-    const int64_t cap = (int64_t)e->sms * bps;
-    const int64_t target = std::max<int64_t>(1, cap * waves);
-    int64_t items = std::max<int64_t>(1, (target + nvs - 1) / nvs);
-    int64_t ppt = std::max<int64_t>(1, (paths + block * items - 1) / (block * items));
-    items = (paths + block * ppt - 1) / (block * ppt);
+    const int64_t cap = std::max<int64_t>(1, (int64_t)e->sms * bps);
+    double best = -1.0;
+    for (int w = 1; w <= 8; ++w) {
+        int64_t it = std::max<int64_t>(1, w * cap / nvs);
+        const int64_t p = std::max<int64_t>(1, (paths + block * it - 1) / (block * it));
+        it = (paths + block * p - 1) / (block * p);
+        const int64_t blocks = nvs * it;
+        const double fill = (double)blocks / (double)(((blocks + cap - 1) / cap) * cap);
+        if (fill > best + 1e-12) {
+            best = fill;
+            *items = it;
+            *ppt = p;
+        }
+        if (fill >= 0.97) break;
+    }
+}
+
+// plan_items, and sizes the partial-sum scratch.
+int plan(lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int nout, Work *w)
+{
+    int64_t items = 1, ppt = 1;
+    plan_items(e, nvs, paths, block, bps, &items, &ppt);
     if (ppt > INT32_MAX || items > INT32_MAX || nvs * items > INT32_MAX)
         return fail(LMM_ERR_TOO_LARGE, "launch too large");
     w->paths = paths;
@@ -212,18 +234,6 @@ int plan(lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int nout
     LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)(nvs * items) * 2 * nout));
     w->partial = e->partial.as<double>();
     return LMM_OK;
-}
-
-// Items/paths-per-thread of a launch without touching the scratch (see plan).
-void plan_items(const lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int64_t *items,
-                int64_t *ppt, int waves = 2)
-{
-    const int64_t cap = (int64_t)e->sms * bps;
-    const int64_t target = std::max<int64_t>(1, cap * waves);
-    int64_t it = std::max<int64_t>(1, (target + nvs - 1) / nvs);
-    int64_t p = std::max<int64_t>(1, (paths + block * it - 1) / (block * it));
-    *ppt = p;
-    *items = (paths + block * p - 1) / (block * p);
 }
 
 int check_paths(int64_t paths)
@@ -584,9 +594,12 @@ int lmm_engine_kernel_time(lmm_engine *e, double *main_kernel_ms, double *total_
     return LMM_OK;
 }
 
-int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops)
+// Times a calibration kernel (16 operations per thread per iteration, 8 x 256
+// threads per SM) for about `ms` milliseconds; returns operations per second.
+static int peak_probe(int32_t device, double ms, const char *what,
+                      const std::function<cudaError_t(int, int, float *, cudaStream_t)> &launch, double *ops_s)
 {
-    if (!tflops || !(ms > 0.0)) return fail(LMM_ERR_INVALID_ARG, "need tflops and ms > 0");
+    if (!ops_s || !(ms > 0.0)) return fail(LMM_ERR_INVALID_ARG, "need an output and ms > 0");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(LMM_ERR_NO_DEVICE, "no CUDA device");
     if (device < 0 || device >= ndev) return fail(LMM_ERR_INVALID_ARG, "device index out of range");
@@ -603,7 +616,7 @@ int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops)
     cudaEventCreate(&b);
     auto run = [&](int iters, float *out_ms) -> cudaError_t {
         cudaEventRecord(a, st);
-        cudaError_t err = lmm::launch_ffma_peak(blocks, iters, 0.9999f, 1e-4f, sink.as<float>(), st);
+        cudaError_t err = launch(blocks, iters, sink.as<float>(), st);
         cudaEventRecord(b, st);
         if (err != cudaSuccess) return err;
         err = cudaEventSynchronize(b);
@@ -621,9 +634,37 @@ int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops)
     cudaEventDestroy(b);
     cudaStreamDestroy(st);
     sink.release();
-    if (err != cudaSuccess) return cuda_fail(err, "FFMA peak probe");
-    const double flops = 2.0 * 16.0 * (double)iters * blocks * 256.0;
-    *tflops = flops / (t * 1e-3) / 1e12;
+    if (err != cudaSuccess) return cuda_fail(err, what);
+    *ops_s = 16.0 * (double)iters * blocks * 256.0 / (t * 1e-3);
+    return LMM_OK;
+}
+
+int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops)
+{
+    if (!tflops) return fail(LMM_ERR_INVALID_ARG, "tflops is NULL");
+    double fma_s = 0.0;
+    LMM_TRY(peak_probe(device, ms, "FFMA peak probe",
+                       [](int blocks, int iters, float *sink, cudaStream_t st) {
+                           return lmm::launch_ffma_peak(blocks, iters, 0.9999f, 1e-4f, sink, st);
+                       },
+                       &fma_s));
+    *tflops = 2.0 * fma_s / 1e12;
+    return LMM_OK;
+}
+
+int lmm_mufu_peak_gops(int32_t device, double ms, double *ex2_gops, double *rcp_gops, double *mixed_gops)
+{
+    double *outs[3] = {ex2_gops, rcp_gops, mixed_gops};
+    for (int kind = 0; kind < 3; ++kind) {
+        if (!outs[kind]) continue;
+        double r = 0.0;
+        LMM_TRY(peak_probe(device, ms, "MUFU peak probe",
+                           [kind](int blocks, int iters, float *sink, cudaStream_t st) {
+                               return lmm::launch_mufu_peak(kind, blocks, iters, sink, st);
+                           },
+                           &r));
+        *outs[kind] = r / 1e9;
+    }
     return LMM_OK;
 }
 

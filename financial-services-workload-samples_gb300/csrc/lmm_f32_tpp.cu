@@ -50,44 +50,21 @@
 #ifndef LMM_TPP_MINB
 #define LMM_TPP_MINB 4
 #endif
-#ifndef LMM_TPP_SEGF
-#define LMM_TPP_SEGF 1
-#endif
-#ifndef LMM_TPP_SEGR
-#define LMM_TPP_SEGR 1
-#endif
 // Reverse steps processed together as a skewed wavefront (independent
 // reconstruction chains per instruction stream): 2 or 4.
 #ifndef LMM_TPP_SKEW
 #define LMM_TPP_SKEW 2
 #endif
-// 1: arrange the reverse cell so that only FFMA -> ex2 -> FFMA -> rcp -> FFMA
-// sits on the reconstruction chain (three more instructions per cell).
-#ifndef LMM_TPP_SHORT
-#define LMM_TPP_SHORT 0
-#endif
-// 0: one unrolled body per step segment (LMM_TPP_SEGF/SEGR). k > 0: a single
-// forward and a single reverse body, entered (forward) or left (reverse) at
-// k-rate chunk boundaries, so the code stays small; each chunk is straight-line.
+// Rates per chunk of the single forward and reverse bodies.
 #ifndef LMM_TPP_CHUNK
 #define LMM_TPP_CHUNK 8
 #endif
-// 1 (with LMM_TPP_CHUNK > 0): in a reverse group, cell (n-g, i+g) uses the
-// maturity constants and vega row of j = i+2g in step n's numbering, so each
-// constant is loaded once per G cells and each vega row gets one
-// read-modify-write per G cells (partial sums kept in registers).
-#ifndef LMM_TPP_WINDOW
-#define LMM_TPP_WINDOW 1
-#endif
-// 1 (with LMM_TPP_CHUNK > 0): forward steps in skewed pairs sharing each
-// constant load (fwd_pair_window).
-#ifndef LMM_TPP_FWD_PAIR
-#define LMM_TPP_FWD_PAIR 1
-#endif
-// 1: the window reverse cell forms y - delta*lambda_k with an FMA instead of
-// reading delta*lambda_k from a table.
-#ifndef LMM_TPP_WIN_NOKX
-#define LMM_TPP_WIN_NOKX 1
+// 1: carry Y = V + sqrt(delta) z as the running drift sum: one add fewer per
+// cell in each phase (4.6% faster on GB300), at the price of accumulating the
+// drift on top of the normal term (FP32 vs FP64 Greek errors about 15% larger,
+// still 1e-6 of the 1e-4 bound).
+#ifndef LMM_TPP_YRUN
+#define LMM_TPP_YRUN 1
 #endif
 
 
@@ -96,6 +73,7 @@ namespace {
 
 constexpr int kTppBlock = LMM_TPP_BLOCK;
 constexpr int kTppMinBlocks = LMM_TPP_MINB;
+constexpr bool kYrun = LMM_TPP_YRUN != 0;
 
 __host__ __device__ constexpr int align16(int x) { return (x + 15) & ~15; }
 
@@ -107,8 +85,7 @@ struct TppLayout {
     static constexpr int PAD = NMAT;                 // k = i-n-1 >= -NMAT
     static constexpr int NOUT = MODE == Mode::Fused ? 1 + 2 * NN : (MODE == Mode::Forward ? 1 : 2 * NN);
     static constexpr int kc = 0;                                     // float4[PAD+NN]
-    static constexpr int kx = kc + 16 * (PAD + NN);                  // float[PAD+NN]
-    static constexpr int l0 = align16(kx + 4 * (PAD + NN));          // float[NN]
+    static constexpr int l0 = align16(kc + 16 * (PAD + NN));         // float[NN]
     static constexpr int il0 = l0 + 4 * NN;                          // float[NN]
     static constexpr int ost = il0 + 4 * NN;                         // int[M+1]
     static constexpr int okf = align16(ost + 4 * (M + 1));           // float[kMaxNopt]
@@ -146,71 +123,146 @@ __device__ __forceinline__ float4 zquad(const float *zp, uint64_t seed, uint64_t
     }
 }
 
-// One forward Euler step over rates I0..NN-1 (path_calc_b1 :63-77).
-// kcn[i] holds the constants of k = i-n-1, zero for k < 0.
-template <int NN, int I0>
-__device__ __forceinline__ float fwd_step(float (&L)[NN], const float4 *kcn, float sqez, float delta)
+// Running drift sum at the start of a step: V = 0, or Y = sqrt(delta) z.
+__device__ __forceinline__ float drift0(float sqez) { return kYrun ? sqez : 0.0f; }
+
+// One forward cell (path_calc_b1 :66-72): drift sum and rate update. k holds
+// the constants of k = i-n-1 (zero for k < 0: an exact no-op).
+__device__ __forceinline__ void fwd_cell(float &L, float &V, const float4 &k, float sqez, float delta)
 {
-    float V = 0.0f;
+    const float r = rcp_approx(fmaf(delta, L, 1.0f));
+    V = fmaf(k.z, L * r, V);
+    L *= ex2_approx(fmaf(k.x, kYrun ? V : V + sqez, k.y));
+}
+
+// One forward step with a single body: rates are grouped in chunks of CH,
+// and the step starts at the chunk holding its first active rate n+1 (cells
+// of that chunk with i <= n are no-ops). Returns the step's drift sum.
+template <int NN, int CH>
+__device__ __forceinline__ float fwd_step_chunked(float (&L)[NN], const float4 *kcn, float sqez,
+                                                  float delta, int n)
+{
+    float V = drift0(sqez);
+    const int c0 = (n + 1) / CH;
 #pragma unroll
-    for (int i = I0; i < NN; ++i) {
-        const float4 k = kcn[i];
-        const float r = rcp_approx(fmaf(delta, L[i], 1.0f));
-        V = fmaf(k.z, L[i] * r, V);
-        L[i] *= ex2_approx(fmaf(k.x, V + sqez, k.y));
+    for (int c = 0; c * CH < NN; ++c) {
+        if (c >= c0) {
+#pragma unroll
+            for (int i = (c * CH < 1 ? 1 : c * CH); i < (c + 1) * CH && i < NN; ++i)
+                fwd_cell(L[i], V, kcn[i], sqez, delta);
+        }
     }
     return V;
 }
 
+// Forward steps n and n+1 with one body over positions p (ascending): cell
+// (n, p) and cell (n+1, p-1). The second finds L_{n+1,p-1} written by cell
+// (n, p-1) one position earlier, so the two drift chains are independent
+// within a position. Cell (n+1, p-1) has k = p-n-3, the constants loaded for
+// cell (n, p-2), so each constant is loaded once per two cells (ring C[j % 3]).
+// Entered at the chunk holding rate n+1; step n+1's cells below its first
+// active rate n+2 see zero constants and are exact no-ops.
+template <int NN, int CH>
+__device__ __forceinline__ void fwd_pair_window(float (&L)[NN], const float4 *kcn, float sqez0,
+                                                float sqez1, float delta, int n, float &V0, float &V1)
+{
+    float4 C[3];
+    V0 = drift0(sqez0);
+    V1 = drift0(sqez1);
+    const int c0 = (n + 1) / CH;
+#pragma unroll
+    for (int c = 0; c * CH < NN; ++c) {
+        if (c >= c0) {
+            if (c == c0) {
+#pragma unroll
+                for (int j = c * CH - 2; j < c * CH; ++j)
+                    if (j >= 0) C[j % 3] = kcn[j];
+            }
+#pragma unroll
+            for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
+                C[p % 3] = kcn[p];
+                if (p >= 1) fwd_cell(L[p], V0, C[p % 3], sqez0, delta);
+                if (p - 1 >= 1) fwd_cell(L[p - 1], V1, C[(p + 1) % 3], sqez1, delta);
+            }
+        }
+    }
+    fwd_cell(L[NN - 1], V1, C[(NN - 2) % 3], sqez1, delta);
+}
+
 struct RevStep {
-    float V, S, sqez;   // S holds delta^2 times the reference's v1
+    float V, S, sqez;   // drift sum, delta^2 times the reference's v1, sqrt(delta) z
     const float4 *kc;   // kc[i]: constants of k = i-n-1
-    const float *kx;    // kx[i]: delta*lambda_k, zero for k < 0
     float *vg;          // vg[i*B]: this thread's vega slot of k = i-n-1
 };
 
-// One reverse cell (path_calc_b2 :105-111 in log-adjoint form) + vega.
-template <int NN, int B>
+// One reverse cell (path_calc_b2 :105-111 in log-adjoint form) + vega, with
+// its constants and vega partial sum passed in from the window.
+template <int NN>
 __device__ __forceinline__ void rev_cell(float (&L)[NN], float (&Pb)[NN], RevStep &s, int i,
-                                         float delta, float d2)
+                                         const float4 &k, float &acc, float delta)
 {
-    const float4 k = s.kc[i];
-    const float dlk = s.kx[i];
-    const float y = s.V + s.sqez;
-#if LMM_TPP_SHORT
-    const float lp = L[i];
-    const float E = ex2_approx(-fmaf(k.x, s.V, fmaf(k.x, s.sqez, k.y)));
-    const float Ln = lp * E;
-    const float r = rcp_approx(fmaf(delta * lp, E, 1.0f));
-    const float t = Ln * r;
-    s.V = fmaf(-(k.z * Ln), r, s.V);
-#else
+    const float y = kYrun ? s.V : s.V + s.sqez;
     const float Ln = L[i] * ex2_approx(-fmaf(k.x, y, k.y));
     const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
     const float t = Ln * r;
     s.V = fmaf(-k.z, t, s.V);
-#endif
     const float pb = Pb[i];
     s.S = fmaf(k.z, pb, s.S);
     const float tS = t * s.S;
-    float *v = s.vg + i * B;
-    *v += fmaf(pb, y - dlk, tS);
+    acc += fmaf(pb, fmaf(-delta, k.w, y), tS);
     Pb[i] = fmaf(k.w * r, tS, pb);
     L[i] = Ln;
 }
 
-// Steps n, n-1, ..., n-G+1 together, step n-g skewed by g rates: at position
-// i the cells (n-g, i+g) are independent of each other, and cell (n-g, i+g)
-// finds L_{n-g+1, i+g} written by cell (n-g+1, i+g) one position earlier.
-template <int NN, int B, int I0, int G>
-__device__ __forceinline__ void rev_group(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
-                                          float delta, float d2)
+// Reverse steps n, n-1, ..., n-G+1 with a single body over positions
+// NN-1 .. -(G-1): cell (n-g, i+g) at position i, which finds
+// L_{n-g+1, i+g} written by cell (n-g+1, i+g) one position earlier. With
+// j = i+2g, the constants of cell (n-g, i+g) are st[0].kc[j] and its vega row
+// is st[0].vg[j*B] (k = j-n-1 of step n): C/A hold them from position j
+// (load) to position j-2(G-1) (last use, vega flush), in rings of 2G-1 slots
+// indexed j mod (2G-1), so that each constant is loaded once and each vega
+// row gets one read-modify-write per G cells. The body is left at the first
+// chunk of CH positions lying wholly below the lowest active position
+// n-2G+3. A vega row is valid (k >= 0) for all or none of its G
+// contributors, and all contributors of a valid row sit at or above that
+// position, so leaving there is exact: the rows still open are spare rows
+// (k < 0), which are never read.
+template <int NN, int B, int G, int CH>
+__device__ __forceinline__ void rev_group_window(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
+                                                 float delta, int n)
 {
+    constexpr int JMAX = NN + G - 2;
+    constexpr int W = 2 * G - 1;
+    const float4 *kc = st[0].kc;
+    float *vg = st[0].vg;
+    float4 C[W];
+    float A[W];
 #pragma unroll
-    for (int i = NN - 1; i >= I0 - (G - 1); --i) {
+    for (int j = NN; j <= JMAX; ++j) {
+        C[j % W] = kc[j];
+        A[j % W] = 0.0f;
+    }
+    const int imin = n - 2 * G + 3;
 #pragma unroll
-        for (int g = 0; g < G; ++g)
-            if (i + g >= I0 && i + g <= NN - 1) rev_cell<NN, B>(L, Pb, st[g], i + g, delta, d2);
+    for (int q = 0; q * CH < NN + G - 1; ++q) {
+        const int top = NN - 1 - q * CH;
+        if (top < imin) return;
+#pragma unroll
+        for (int i = top; i > top - CH && i >= -(G - 1); --i) {
+            if (i >= 1) {
+                C[i % W] = kc[i];
+                A[i % W] = 0.0f;
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (i + g >= 1 && i + g <= NN - 1) {
+                    const int j = i + 2 * g;
+                    rev_cell<NN>(L, Pb, st[g], i + g, C[j % W], A[j % W], delta);
+                }
+            }
+            const int jf = i + 2 * (G - 1);
+            if (jf >= 1 && jf <= JMAX) vg[jf * B] += A[jf % W];
+        }
     }
 }
 
@@ -310,259 +362,69 @@ __device__ __forceinline__ void column_reduce(const float *vg, int warp, int lan
     }
 }
 
-// One forward step with a single body: rates are grouped in chunks of CH,
-// and the step starts at the chunk holding its first active rate n+1 (cells
-// of that chunk with i <= n are no-ops).
-template <int NN, int CH>
-__device__ __forceinline__ float fwd_step_chunked(float (&L)[NN], const float4 *kcn, float sqez,
-                                                  float delta, int n)
-{
-    float V = 0.0f;
-    const int c0 = (n + 1) / CH;
-#pragma unroll
-    for (int c = 0; c * CH < NN; ++c) {
-        if (c >= c0) {
-#pragma unroll
-            for (int i = (c * CH < 1 ? 1 : c * CH); i < (c + 1) * CH && i < NN; ++i) {
-                const float4 k = kcn[i];
-                const float r = rcp_approx(fmaf(delta, L[i], 1.0f));
-                V = fmaf(k.z, L[i] * r, V);
-                L[i] *= ex2_approx(fmaf(k.x, V + sqez, k.y));
-            }
-        }
-    }
-    return V;
-}
-
-// One forward cell (path_calc_b1 :66-72): drift sum and rate update.
-__device__ __forceinline__ void fwd_cell(float &L, float &V, const float4 &k, float sqez, float delta)
-{
-    const float r = rcp_approx(fmaf(delta, L, 1.0f));
-    V = fmaf(k.z, L * r, V);
-    L *= ex2_approx(fmaf(k.x, V + sqez, k.y));
-}
-
-// Forward steps n and n+1 with one body over positions p (ascending): cell
-// (n, p) and cell (n+1, p-1). The second finds L_{n+1,p-1} written by cell
-// (n, p-1) one position earlier, so the two drift chains are independent
-// within a position. Cell (n+1, p-1) has k = p-n-3, the constants loaded for
-// cell (n, p-2), so each constant is loaded once per two cells (C[] keeps
-// three). Entered at the chunk holding rate n+1; step n+1's cells below its
-// first active rate n+2 see zero constants and are exact no-ops.
-template <int NN, int CH>
-__device__ __forceinline__ void fwd_pair_window(float (&L)[NN], const float4 *kcn, float sqez0,
-                                                float sqez1, float delta, int n, float &V0, float &V1)
-{
-    float4 C[3];  // ring: C[j % 3] holds the constants of position j
-    V0 = 0.0f;
-    V1 = 0.0f;
-    const int c0 = (n + 1) / CH;
-#pragma unroll
-    for (int c = 0; c * CH < NN; ++c) {
-        if (c >= c0) {
-            if (c == c0) {
-#pragma unroll
-                for (int j = c * CH - 2; j < c * CH; ++j)
-                    if (j >= 0) C[j % 3] = kcn[j];
-            }
-#pragma unroll
-            for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
-                C[p % 3] = kcn[p];
-                if (p >= 1) fwd_cell(L[p], V0, C[p % 3], sqez0, delta);
-                if (p - 1 >= 1) fwd_cell(L[p - 1], V1, C[(p + 1) % 3], sqez1, delta);
-            }
-        }
-    }
-    fwd_cell(L[NN - 1], V1, C[(NN - 2) % 3], sqez1, delta);
-}
-
-// A group of G reverse steps n..n-G+1 with a single body over positions
-// NN-1 .. -(G-1) (cell (n-g, i+g) at position i), left at the first chunk of
-// CH positions lying wholly below the lowest active position n-2G+3.
-template <int NN, int B, int G, int CH>
-__device__ __forceinline__ void rev_group_chunked(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
-                                                  float delta, float d2, int n)
-{
-    const int imin = n - 2 * G + 3;
-#pragma unroll
-    for (int q = 0; q * CH < NN + G - 1; ++q) {
-        const int top = NN - 1 - q * CH;
-        if (top < imin) break;
-#pragma unroll
-        for (int i = top; i > top - CH && i >= -(G - 1); --i) {
-#pragma unroll
-            for (int g = 0; g < G; ++g)
-                if (i + g >= 1 && i + g <= NN - 1) rev_cell<NN, B>(L, Pb, st[g], i + g, delta, d2);
-        }
-    }
-}
-
-// Reverse cell with its constants and vega accumulator passed in (window form).
-template <int NN>
-__device__ __forceinline__ void rev_cell_w(float (&L)[NN], float (&Pb)[NN], RevStep &s, int i,
-                                           const float4 &k, float dlk, float &acc, float delta)
-{
-    const float y = s.V + s.sqez;
-    const float Ln = L[i] * ex2_approx(-fmaf(k.x, y, k.y));
-    const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
-    const float t = Ln * r;
-    s.V = fmaf(-k.z, t, s.V);
-    const float pb = Pb[i];
-    s.S = fmaf(k.z, pb, s.S);
-    const float tS = t * s.S;
-#if LMM_TPP_WIN_NOKX
-    acc += fmaf(pb, fmaf(-delta, k.w, y), tS);
-#else
-    acc += fmaf(pb, y - dlk, tS);
-#endif
-    Pb[i] = fmaf(k.w * r, tS, pb);
-    L[i] = Ln;
-}
-
-// Window form of rev_group_chunked. With j = i+2g, the constants of cell
-// (n-g, i+g) are st[0].kc[j] and its vega row is st[0].vg[j*B] (k = j-n-1
-// of step n): C/D/A hold them from position j (load) to position j-2(G-1)
-// (last use, vega flush), in rings of 2G-1 slots indexed j mod (2G-1). A
-// vega row is valid (k >= 0) for all or none of its G contributors, and all
-// contributors of a valid row sit at or above the lowest active position
-// n-2G+3, so leaving at a chunk boundary below it is exact: the rows still
-// open then are spare rows (k < 0), which are never read.
-template <int NN, int B, int G, int CH>
-__device__ __forceinline__ void rev_group_window(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
-                                                 float delta, int n)
-{
-    constexpr int JMAX = NN + G - 2;
-    constexpr int W = 2 * G - 1;
-    const float4 *kc = st[0].kc;
-    const float *kx = st[0].kx;
-    float *vg = st[0].vg;
-    float4 C[W];
-    float D[W], A[W];
-#pragma unroll
-    for (int j = NN; j <= JMAX; ++j) {
-        C[j % W] = kc[j];
-        D[j % W] = LMM_TPP_WIN_NOKX ? 0.0f : kx[j];
-        A[j % W] = 0.0f;
-    }
-    const int imin = n - 2 * G + 3;
-#pragma unroll
-    for (int q = 0; q * CH < NN + G - 1; ++q) {
-        const int top = NN - 1 - q * CH;
-        if (top < imin) return;
-#pragma unroll
-        for (int i = top; i > top - CH && i >= -(G - 1); --i) {
-            if (i >= 1) {
-                C[i % W] = kc[i];
-                D[i % W] = LMM_TPP_WIN_NOKX ? 0.0f : kx[i];
-                A[i % W] = 0.0f;
-            }
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                if (i + g >= 1 && i + g <= NN - 1) {
-                    const int j = i + 2 * g;
-                    rev_cell_w<NN>(L, Pb, st[g], i + g, C[j % W], D[j % W], A[j % W], delta);
-                }
-            }
-            const int jf = i + 2 * (G - 1);
-            if (jf >= 1 && jf <= JMAX) vg[jf * B] += A[jf % W];
-        }
-    }
-}
-
-// Forward over all steps, segment by segment (segment s: steps [lo, hi),
-// body over rates lo+1..NN-1).
-template <int NN, int NMAT, int SEG, bool PHILOX, Mode MODE, int S = 0>
+// Forward over all steps. The fused kernel runs steps in skewed pairs; the
+// forward-only kernel runs single steps (the pair's extra live constants
+// cost it more occupancy than they save) and writes the tape.
+template <int NN, int NMAT, bool PHILOX, Mode MODE>
 __device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, float4 &zq,
                                             float4 &zq_next, const float *zp, uint64_t seed,
                                             uint64_t gpath, float sqd, float delta, float *vt_s,
                                             float *tape_v, int64_t total, bool active)
 {
-    if constexpr (S < SEG) {
-        constexpr int lo = S * NMAT / SEG, hi = (S + 1) * NMAT / SEG;
-        constexpr int B = kTppBlock;
-#if LMM_TPP_CHUNK > 0 && LMM_TPP_FWD_PAIR
-        // Paired steps in the fused kernel only: in the forward-only kernel the
-        // pair's extra live constants cost more occupancy than they save.
-        constexpr bool pair = MODE == Mode::Fused;
-#else
-        constexpr bool pair = false;
-#endif
-        if constexpr (pair) {
-            static_assert(SEG == 1 && NMAT % 2 == 0, "paired forward steps run over all steps");
-            for (int n = 0; n < NMAT; n += 2) {
-                if ((n & 3) == 0) {
-                    zq = zq_next;
-                    if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
-                }
-                const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
-                const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
-                float V0, V1;
-                fwd_pair_window<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez0, sqez1, delta, n, V0, V1);
-                vt_s[n * B] = V0;
-                vt_s[(n + 1) * B] = V1;
+    constexpr int B = kTppBlock;
+    if constexpr (MODE == Mode::Fused) {
+        static_assert(NMAT % 2 == 0, "paired forward steps");
+        for (int n = 0; n < NMAT; n += 2) {
+            if ((n & 3) == 0) {
+                zq = zq_next;
+                if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
             }
-        } else {
-            for (int n = lo; n < hi; ++n) {
-                if ((n & 3) == 0) {
-                    zq = zq_next;
-                    if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
-                }
-                const float sqez = sqd * pick4(zq, n & 3);
-#if LMM_TPP_CHUNK > 0
-                const float V = fwd_step_chunked<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez, delta, n);
-#else
-                const float V = fwd_step<NN, lo + 1>(L, kc0 - (n + 1), sqez, delta);
-#endif
-                if (MODE == Mode::Fused)
-                    vt_s[n * B] = V;
-                else if (active)
-                    tape_v[(int64_t)n * total] = V;
-            }
+            const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
+            const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
+            float V0, V1;
+            fwd_pair_window<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez0, sqez1, delta, n, V0, V1);
+            vt_s[n * B] = V0;
+            vt_s[(n + 1) * B] = V1;
         }
-        forward_all<NN, NMAT, SEG, PHILOX, MODE, S + 1>(L, kc0, zq, zq_next, zp, seed, gpath, sqd,
-                                                        delta, vt_s, tape_v, total, active);
+    } else {
+        for (int n = 0; n < NMAT; ++n) {
+            if ((n & 3) == 0) {
+                zq = zq_next;
+                if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+            }
+            const float sqez = sqd * pick4(zq, n & 3);
+            const float V = fwd_step_chunked<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez, delta, n);
+            if (active) tape_v[(int64_t)n * total] = V;
+        }
     }
 }
 
-// Reverse over all steps, segments from the last, pairs (n, n-1) within each.
-template <int NN, int NMAT, int SEG, bool PHILOX, Mode MODE, int S = SEG - 1>
+// Reverse over all steps, in groups of G steps from the last.
+template <int NN, int NMAT, bool PHILOX, Mode MODE>
 __device__ __forceinline__ void reverse_all(float (&L)[NN], float (&Pb)[NN], const float4 *kc0,
-                                            const float *kx0, float *vg0, float4 &zq,
-                                            float4 &zq_next, const float *zp, uint64_t seed,
-                                            uint64_t gpath, float sqd, float delta, float d2,
+                                            float *vg0, float4 &zq, float4 &zq_next, const float *zp,
+                                            uint64_t seed, uint64_t gpath, float sqd, float delta,
                                             const float *vt_s, const float *tape_v, int64_t total)
 {
-    if constexpr (S >= 0) {
-        constexpr int lo = S * NMAT / SEG, hi = (S + 1) * NMAT / SEG;
-        constexpr int G = LMM_TPP_SKEW;
-        static_assert((hi - lo) % G == 0 && (G == 2 || G == 4), "reverse segments hold whole step groups");
-        constexpr int B = kTppBlock;
-        for (int n = hi - 1; n > lo; n -= G) {
-            if ((n & 3) == 3) {
-                zq = zq_next;
-                if ((n >> 2) > 0) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) - 1);
-            }
-            RevStep st[G];
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                const int m = n - g;
-                st[g].sqez = sqd * pick4(zq, m & 3);
-                st[g].V = MODE == Mode::Fused ? vt_s[m * B] : tape_v[(int64_t)m * total];
-                st[g].S = 0.0f;
-                st[g].kc = kc0 - (m + 1);
-                st[g].kx = kx0 - (m + 1);
-                st[g].vg = vg0 - (m + 1) * B;
-            }
-#if LMM_TPP_CHUNK > 0 && LMM_TPP_WINDOW
-            rev_group_window<NN, B, G, LMM_TPP_CHUNK>(L, Pb, st, delta, n);
-#elif LMM_TPP_CHUNK > 0
-            rev_group_chunked<NN, B, G, LMM_TPP_CHUNK>(L, Pb, st, delta, d2, n);
-#else
-            rev_group<NN, B, lo + 1, G>(L, Pb, st, delta, d2);
-#endif
+    constexpr int G = LMM_TPP_SKEW;
+    static_assert(NMAT % G == 0 && (G == 2 || G == 4), "whole step groups");
+    constexpr int B = kTppBlock;
+    for (int n = NMAT - 1; n > 0; n -= G) {
+        if ((n & 3) == 3) {
+            zq = zq_next;
+            if ((n >> 2) > 0) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) - 1);
         }
-        reverse_all<NN, NMAT, SEG, PHILOX, MODE, S - 1>(L, Pb, kc0, kx0, vg0, zq, zq_next, zp, seed,
-                                                        gpath, sqd, delta, d2, vt_s, tape_v, total);
+        RevStep st[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int m = n - g;
+            st[g].sqez = sqd * pick4(zq, m & 3);
+            st[g].V = MODE == Mode::Fused ? vt_s[m * B] : tape_v[(int64_t)m * total];
+            st[g].S = 0.0f;
+            st[g].kc = kc0 - (m + 1);
+            st[g].vg = vg0 - (m + 1) * B;
+        }
+        rev_group_window<NN, B, G, LMM_TPP_CHUNK>(L, Pb, st, delta, n);
     }
 }
 
@@ -576,7 +438,6 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     static_assert(NMAT % 4 == 0, "normals are read in aligned quads");
     extern __shared__ __align__(16) unsigned char smem[];
     float4 *kc_s = reinterpret_cast<float4 *>(smem + Lay::kc);
-    float *kx_s = reinterpret_cast<float *>(smem + Lay::kx);
     float *l0_s = reinterpret_cast<float *>(smem + Lay::l0);
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
@@ -593,7 +454,6 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     for (int i = tid; i < PAD + NN; i += B) {
         const int k = i - PAD;
         kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
-        kx_s[i] = k < 0 ? 0.0f : m.kd[k];
     }
     for (int i = tid; i < NN; i += B) {
         l0_s[i] = m.L0f[scen * NN + i];
@@ -610,12 +470,11 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     for (int i = tid; i < Lay::NW * 2 * NOUT; i += B) acc_s[i] = 0.0;
     __syncthreads();
 
-    const float delta = m.delta, sqd = m.sqd, d2 = m.d2;
+    const float delta = m.delta, sqd = m.sqd;
     const int64_t total = (int64_t)m.nscen * w.paths;
     const int64_t ibase = (int64_t)item * w.ppt * B;
     const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
     const float4 *kc0 = kc_s + PAD;
-    const float *kx0 = kx_s + PAD;
     float *vg0 = vg_s + PAD * B + tid;
     float *vt0 = vt_s + tid;
 
@@ -637,8 +496,8 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 #pragma unroll
             for (int i = 0; i < NN; ++i) L[i] = l0_s[i];
             zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
-            forward_all<NN, NMAT, LMM_TPP_SEGF, PHILOX, MODE>(L, kc0, zq, zq_next, zp, seed, gpath, sqd,
-                                                              delta, vt0, tape_v, total, active);
+            forward_all<NN, NMAT, PHILOX, MODE>(L, kc0, zq, zq_next, zp, seed, gpath, sqd, delta, vt0,
+                                                tape_v, total, active);
             if (MODE == Mode::Forward && active) {
 #pragma unroll
                 for (int i = 0; i < NN; ++i) tape[(int64_t)i * total + tp] = L[i];
@@ -659,8 +518,8 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 #pragma unroll
             for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
             zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);
-            reverse_all<NN, NMAT, LMM_TPP_SEGR, PHILOX, MODE>(L, Pb, kc0, kx0, vg0, zq, zq_next, zp, seed,
-                                                              gpath, sqd, delta, d2, vt0, tape_v, total);
+            reverse_all<NN, NMAT, PHILOX, MODE>(L, Pb, kc0, vg0, zq, zq_next, zp, seed, gpath, sqd, delta,
+                                                vt0, tape_v, total);
         }
 
         // ---- cross-path reduction of this batch of B paths ----

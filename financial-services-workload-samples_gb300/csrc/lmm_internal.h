@@ -84,6 +84,8 @@ cudaError_t launch_bump_diff(double *mean, double *se, int nscen, int nout, doub
 // FFMA throughput probe: `blocks` x 256 threads, `iters` iterations of 16
 // independent FMA chains each; one float per thread to `sink`.
 cudaError_t launch_ffma_peak(int blocks, int iters, float a, float b, float *sink, cudaStream_t s);
+// kind 0: ex2.approx, 1: rcp.approx, 2: both alternately; 16 per thread per iteration
+cudaError_t launch_mufu_peak(int kind, int blocks, int iters, float *sink, cudaStream_t s);
 
 // MRG32k3a jump tables (lmm_mrg.cu): A1^(2^k), A2^(2^k) for k < 64 and the
 // per-lane offsets A1^(l*span), A2^(l*span) for l < 32, entries mod m1/m2.

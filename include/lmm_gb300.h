@@ -111,6 +111,13 @@ int lmm_engine_kernel_time(lmm_engine *e, double *main_kernel_ms, double *total_
  * FMA) of `device`, from a register-resident FMA-chain kernel timed with CUDA
  * events over about `ms` milliseconds. */
 int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops);
+/* Measured special-function (MUFU) throughput on `device`, in 10^9 operations
+ * per second, for ex2.approx, rcp.approx and the two alternating (the mix the
+ * LMM cells issue: one exp and one reciprocal per cell), each from an
+ * independent-chain kernel run for about `ms` milliseconds. Any output may
+ * be NULL. The roofline of the FP32 kernels against the MUFU pipe. */
+int lmm_mufu_peak_gops(int32_t device, double ms, double *ex2_gops, double *rcp_gops,
+                       double *mixed_gops);
 
 /* ---- value + all Greeks, FP32 adjoint (the fast path) ----------------- */
 /* Replaces the per-path work of liborSwaptionGreeks.cpp:281-344 (forward,
