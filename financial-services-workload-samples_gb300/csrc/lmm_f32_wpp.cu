@@ -32,7 +32,7 @@ __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(
 // Shared-memory layout (bytes), shared by host and device.
 struct WppLay {
     int nn, nmat, S, nck, nout, M;
-    size_t kc, kd, l0, il0, ost, okf, okd, owf, owd, warp0, per_warp, ck, vg, lw, bw, acc, bytes;
+    size_t kc, l0, il0, ost, okf, okd, owf, owd, warp0, per_warp, ck, vg, lw, bw, acc, bytes;
 };
 
 __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
@@ -45,8 +45,7 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
     L.nck = (nmat + kWppCkpt - 1) / kWppCkpt;
     L.nout = 1 + 2 * nn;
     size_t o = 0;
-    L.kc = o; o = al16(o + 16 * (size_t)nn);
-    L.kd = o; o = al16(o + 4 * (size_t)nn);
+    L.kc = o; o = al16(o + 16 * (size_t)(nn + 1));    // [0]: zeros, [k+1]: constants of k
     L.l0 = o; o = al16(o + 4 * (size_t)nn);
     L.il0 = o; o = al16(o + 4 * (size_t)nn);
     L.ost = o; o = al16(o + 4 * (size_t)(L.M + 1));
@@ -57,7 +56,7 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
     L.warp0 = o;
     size_t w = 0;
     L.ck = w; w = al16(w + 4 * (size_t)L.nck * 32 * S);   // checkpoints [nck][32*S]
-    L.vg = w; w = al16(w + 4 * (size_t)32 * S);           // vegas [32*S] (index k)
+    L.vg = w; w = al16(w + 4 * (size_t)(32 * S + 1));     // vegas [1+32*S] (row k+1; row 0 discards)
     L.lw = w; w = al16(w + 4 * (size_t)32 * S);           // payoff staging [32*S]
     L.bw = w; w = al16(w + 4 * (size_t)32 * S);           // annuity factors B[m] [32*S]
     L.acc = w; w = al16(w + 8 * (size_t)2 * L.nout);      // FP64 sums [2*nout]
@@ -93,75 +92,75 @@ __device__ __forceinline__ float warp_excl_suffix(float x, int lane)
     return lane == 31 ? 0.0f : ex;
 }
 
-// One forward step n over the lane's slots. If T/Vs are given, the cell's
-// pre-step rate and inclusive drift sum are kept (for the recompute of a
-// checkpoint segment). The rate, not t = L/(1+delta L), is kept: forming
-// r = 1/(1+delta L) again as 1 - delta t would cancel catastrophically on
-// paths whose rates grow large.
+// Constants and vega row of slot s at step n: row max(base[s] - n, 0) of the
+// tables, whose row 0 is zero (constants) or discarded (vegas) and row k+1
+// holds k. base[s] = i for a real rate i < nn (row i-n = k+1 for k = i-n-1
+// >= 0, row 0 for a rate not yet moving), 0 for a padding slot (i >= nn). A
+// zero row makes the cell an exact no-op: L *= 2^0, the sums gain 0 and Pb
+// keeps its value, so the steps need no per-slot branches.
 template <int S>
-__device__ __forceinline__ void wpp_fwd_step(float (&L)[S], int n, float sqez, int lane, int nn,
-                                             const float4 *kc, float delta, float (*T), float (*Vs))
+__device__ __forceinline__ int wpp_row(const int (&base)[S], int s, int n)
 {
-    float a[S], Lpre[S];
+    return max(base[s] - n, 0);
+}
+
+// One forward step n over the lane's slots. If T/Vs are given, the cell's
+// pre-step rate and its drift sum plus sqrt(delta) z are kept (for the
+// recompute of a checkpoint segment). The rate, not t = L/(1+delta L), is
+// kept: forming r = 1/(1+delta L) again as 1 - delta t would cancel
+// catastrophically on paths whose rates grow large.
+template <int S>
+__device__ __forceinline__ void wpp_fwd_step(float (&L)[S], const int (&base)[S], int n, float sqez,
+                                             int lane, const float4 *kc, float delta, float *T, float *Vs)
+{
+    float a[S];
     float4 kk[S];
     float P = 0.0f;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-        const int i = S * lane + s;
-        const bool act = i > n && i < nn;
-        kk[s] = kc[act ? i - n - 1 : 0];
+        kk[s] = kc[wpp_row(base, s, n)];
         const float r = rcp_approx(fmaf(delta, L[s], 1.0f));
-        Lpre[s] = L[s];
-        a[s] = act ? kk[s].z * (L[s] * r) : 0.0f;
-        P += a[s];
+        P = fmaf(kk[s].z, L[s] * r, P);
         a[s] = P;                                   // local inclusive prefix
     }
-    const float X = warp_excl_prefix(P, lane);
+    const float X = warp_excl_prefix(P, lane) + sqez;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-        const int i = S * lane + s;
-        const bool act = i > n && i < nn;
-        const float V = X + a[s];
-        if (act) L[s] *= ex2_approx(fmaf(kk[s].x, V + sqez, kk[s].y));
+        const float Y = X + a[s];                   // V_i + sqrt(delta) z
         if (T) {
-            T[s] = Lpre[s];
-            Vs[s] = V;
+            T[s] = L[s];
+            Vs[s] = Y;
         }
+        L[s] *= ex2_approx(fmaf(kk[s].x, Y, kk[s].y));
     }
 }
 
 // Adjoint of step n (path_calc_b2 :100-112 in log-adjoint form) + vega.
 template <int S>
-__device__ __forceinline__ void wpp_rev_step(float (&Pb)[S], int n, float sqez, int lane, int nn,
-                                             const float4 *kc, const float *kd, float *vg,
-                                             const float *T, const float *Vs, float delta, float d2)
+__device__ __forceinline__ void wpp_rev_step(float (&Pb)[S], const int (&base)[S], int n, int lane,
+                                             const float4 *kc, float *vg, const float *T, const float *Vs,
+                                             float delta, float d2)
 {
     float b[S];
+    float4 kk[S];
     float Q = 0.0f;
 #pragma unroll
     for (int s = S - 1; s >= 0; --s) {
-        const int i = S * lane + s;
-        const bool act = i > n && i < nn;
-        const float lam = act ? kc[i - n - 1].w : 0.0f;
-        Q = fmaf(lam, Pb[s], Q);
+        kk[s] = kc[wpp_row(base, s, n)];
+        Q = fmaf(kk[s].w, Pb[s], Q);
         b[s] = Q;                                   // local inclusive suffix
     }
     const float Y = warp_excl_suffix(Q, lane);
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-        const int i = S * lane + s;
-        if (i > n && i < nn) {
-            const int k = i - n - 1;
-            const float4 kk = kc[k];
-            const float Ssum = Y + b[s];
-            const float r = rcp_approx(fmaf(delta, T[s], 1.0f));
-            const float t = T[s] * r;
-            const float tS = t * Ssum;
-            vg[k] += fmaf(Pb[s], Vs[s] + sqez - kd[k], d2 * tS);
-            Pb[s] = fmaf(kk.z * r, tS, Pb[s]);
-        }
+        const float Ssum = Y + b[s];
+        const float r = rcp_approx(fmaf(delta, T[s], 1.0f));
+        const float t = T[s] * r;
+        const float tS = t * Ssum;
+        vg[wpp_row(base, s, n)] += fmaf(Pb[s], fmaf(-delta, kk[s].w, Vs[s]), d2 * tS);
+        Pb[s] = fmaf(kk[s].z * r, tS, Pb[s]);
     }
-    // The next step's vega slots overlap neighbouring lanes' slots of this
+    // The next step's vega rows overlap neighbouring lanes' rows of this
     // step: order the shared-memory read-modify-writes across the warp.
     __syncwarp();
 }
@@ -209,7 +208,6 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     const WppLay Ly = wpp_layout(nn, nmat, S);
     const int M = Ly.M, nout = Ly.nout;
     float4 *kc_s = reinterpret_cast<float4 *>(smem + Ly.kc);
-    float *kd_s = reinterpret_cast<float *>(smem + Ly.kd);
     float *l0_s = reinterpret_cast<float *>(smem + Ly.l0);
     float *il0_s = reinterpret_cast<float *>(smem + Ly.il0);
     int *ost_s = reinterpret_cast<int *>(smem + Ly.ost);
@@ -226,9 +224,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     double *acc = reinterpret_cast<double *>(wbase + Ly.acc);
 
     const int scen = blockIdx.x / w.items, item = blockIdx.x % w.items;
+    for (int i = tid; i <= nn; i += kWppBlock) kc_s[i] = i == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[i - 1];
     for (int i = tid; i < nn; i += kWppBlock) {
-        kc_s[i] = m.kc[i];
-        kd_s[i] = m.kd[i];
         l0_s[i] = m.L0f[scen * nn + i];
         il0_s[i] = m.invL0f[scen * nn + i];
     }
@@ -240,8 +237,15 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         owd_s[i] = m.optWd[i];
     }
     for (int i = lane; i < 2 * nout; i += 32) acc[i] = 0.0;
-    for (int i = lane; i < 32 * S; i += 32) vg_s[i] = 0.0f;
+    for (int i = lane; i <= 32 * S; i += 32) vg_s[i] = 0.0f;
     __syncthreads();
+
+    int base[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int i = S * lane + s;
+        base[s] = i < nn ? i : 0;
+    }
 
     const float delta = m.delta, sqd = m.sqd, d2 = m.d2;
     const int64_t ibase = (int64_t)item * w.ppt * kWppWarps;
@@ -265,7 +269,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 for (int s = 0; s < S; ++s) ck_s[(n / kWppCkpt) * 32 * S + S * lane + s] = L[s];
             }
             const float sqez = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
-            wpp_fwd_step<S>(L, n, sqez, lane, nn, kc_s, delta, nullptr, nullptr);
+            wpp_fwd_step<S>(L, base, n, sqez, lane, kc_s, delta, nullptr, nullptr);
         }
         // ---- payoff (FP64 products) and its adjoint ----
         double dprod = 1.0;
@@ -336,13 +340,13 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 const int n = c * kWppCkpt + jj;
                 if (n < nmat) {
                     zs[jj] = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
-                    wpp_fwd_step<S>(L, n, zs[jj], lane, nn, kc_s, delta, T[jj], Vs[jj]);
+                    wpp_fwd_step<S>(L, base, n, zs[jj], lane, kc_s, delta, T[jj], Vs[jj]);
                 }
             }
 #pragma unroll
             for (int jj = kWppCkpt - 1; jj >= 0; --jj) {
                 const int n = c * kWppCkpt + jj;
-                if (n < nmat) wpp_rev_step<S>(Pb, n, zs[jj], lane, nn, kc_s, kd_s, vg_s, T[jj], Vs[jj], delta, d2);
+                if (n < nmat) wpp_rev_step<S>(Pb, base, n, lane, kc_s, vg_s, T[jj], Vs[jj], delta, d2);
             }
         }
         // ---- accumulate this path: value, deltas, vegas ----
@@ -361,10 +365,10 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             }
         }
         for (int k = lane; k < nn; k += 32) {
-            const double vgk = (double)vg_s[k];
+            const double vgk = (double)vg_s[k + 1];
             acc[1 + nn + k] += vgk;
             acc[nout + 1 + nn + k] += vgk * vgk;
-            vg_s[k] = 0.0f;
+            vg_s[k + 1] = 0.0f;
         }
         __syncwarp();
     }
