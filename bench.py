@@ -47,6 +47,9 @@ PROFILE_JSON = os.path.join(ROOT, "profiles", "lmm_fused_f32_80x40.json")
 #   portfolio_b :120-211                        ~900 per path
 OPS_PER_CELL = 32
 OPS_PORTFOLIO = 900
+# One FP64 forward revaluation (the bump comparator's unit of work): the
+# forward cell of :68-73 (11 operations) over the triangle plus the portfolio.
+OPS_FWD_CELL = 11
 # Special-function (MUFU) operations per path: each cell issues one ex2 and one
 # reciprocal in the forward and again in the reverse reconstruction; the
 # payoff and its adjoint take 2*NN reciprocals.
@@ -382,7 +385,13 @@ def run_ours(args):
         s1.record(stream)
         torch.cuda.synchronize(dev)
         bt = s0.elapsed_time(s1) / 1e3
+        f64_peak = P.fp64_peak_tflops(local, 200.0)
+        bump_ops = (OPS_FWD_CELL * cells(cfg.nn, nmat) + OPS_PORTFOLIO) * (1 + 2 * cfg.nn) * nb
         bump = {"paths_per_s": nb / bt, "sample_paths": nb, "forward_runs": 1 + 2 * cfg.nn,
+                "roofline": {"bound": "fp64", "achieved": bump_ops / bt / 1e12, "peak": f64_peak,
+                             "unit": "TFLOP/s", "frac": bump_ops / bt / 1e12 / f64_peak,
+                             "ops_per_forward_run": OPS_FWD_CELL * cells(cfg.nn, nmat) + OPS_PORTFOLIO,
+                             "peak_source": "measured live: DFMA-chain kernel lmm_fp64_peak_tflops"},
                 "seconds": bt, "method": "FP64 forward re-run per bumped input (one-sided, h=1e-6)",
                 "fp32_adjoint_speedup": value / ws / (nb / bt)}
 

@@ -36,7 +36,7 @@ EXPORTS = (
     "lmm_mrg32k3a_uniforms_device", "lmm_mrg32k3a_normals_f64_device", "lmm_mrg32k3a_normals_f32_device",
     "lmm_swaption_greeks_mrg32k3a", "lmm_swaption_greeks_mrg32k3a_f32",
     "lmm_engine_set_weights", "lmm_swaption_breakdown_f32_device", "lmm_swaption_breakdown_f64_device",
-    "lmm_mufu_peak_gops",
+    "lmm_mufu_peak_gops", "lmm_fp64_peak_tflops",
 )
 
 
@@ -87,6 +87,7 @@ def lib():
         "lmm_engine_kernel_time": ([vp, dp, dp], C.c_int),
         "lmm_fp32_peak_tflops": ([i32, C.c_double, dp], C.c_int),
         "lmm_mufu_peak_gops": ([i32, C.c_double, dp, dp, dp], C.c_int),
+        "lmm_fp64_peak_tflops": ([i32, C.c_double, dp], C.c_int),
         "lmm_greeks_f32_host": ([vp, fp, i64, dp, dp], C.c_int),
         "lmm_greeks_f32_device": ([vp, vp, i64, vp, vp], C.c_int),
         "lmm_greeks_philox_host": ([vp, u64, i64, i64, dp, dp], C.c_int),
@@ -314,6 +315,13 @@ def fp32_peak_tflops(device: int = 0, ms: float = 200.0) -> float:
     """Measured FP32 FMA throughput of the device (roofline denominator)."""
     t = C.c_double()
     _check(lib().lmm_fp32_peak_tflops(device, ms, C.byref(t)), "lmm_fp32_peak_tflops")
+    return t.value
+
+
+def fp64_peak_tflops(device: int = 0, ms: float = 200.0) -> float:
+    """Measured FP64 FMA throughput of the device (FP64 kernels' roofline)."""
+    t = C.c_double()
+    _check(lib().lmm_fp64_peak_tflops(device, ms, C.byref(t)), "lmm_fp64_peak_tflops")
     return t.value
 
 

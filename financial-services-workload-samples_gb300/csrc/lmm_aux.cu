@@ -118,6 +118,22 @@ __global__ void __launch_bounds__(256) k_ffma_peak(int iters, float a, float b, 
     sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// FP64 FMA throughput probe: 16 independent DFMA chains per thread.
+__global__ void __launch_bounds__(256) k_dfma_peak(int iters, double a, double b, float *sink)
+{
+    double x[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) x[j] = (double)(threadIdx.x + j) * 1e-3;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) x[j] = fma(x[j], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) s += x[j];
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = (float)s;
+}
+
 // MUFU throughput probe: 16 independent chains per thread of ex2 (KIND 0:
 // x = 2^-x, which stays in (1/2, 1)), rcp (KIND 1: x = 1/(1+x), which tends
 // to 0.618; x = 1/x would be folded away) or both alternately (KIND 2), so
@@ -172,6 +188,12 @@ cudaError_t launch_bump_diff(double *mean, double *se, int nscen, int nout, doub
 cudaError_t launch_ffma_peak(int blocks, int iters, float a, float b, float *sink, cudaStream_t s)
 {
     k_ffma_peak<<<blocks, 256, 0, s>>>(iters, a, b, sink);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dfma_peak(int blocks, int iters, double a, double b, float *sink, cudaStream_t s)
+{
+    k_dfma_peak<<<blocks, 256, 0, s>>>(iters, a, b, sink);
     return cudaGetLastError();
 }
 

@@ -84,6 +84,7 @@ cudaError_t launch_bump_diff(double *mean, double *se, int nscen, int nout, doub
 // FFMA throughput probe: `blocks` x 256 threads, `iters` iterations of 16
 // independent FMA chains each; one float per thread to `sink`.
 cudaError_t launch_ffma_peak(int blocks, int iters, float a, float b, float *sink, cudaStream_t s);
+cudaError_t launch_dfma_peak(int blocks, int iters, double a, double b, float *sink, cudaStream_t s);
 // kind 0: ex2.approx, 1: rcp.approx, 2: both alternately; 16 per thread per iteration
 cudaError_t launch_mufu_peak(int kind, int blocks, int iters, float *sink, cudaStream_t s);
 

@@ -111,6 +111,8 @@ int lmm_engine_kernel_time(lmm_engine *e, double *main_kernel_ms, double *total_
  * FMA) of `device`, from a register-resident FMA-chain kernel timed with CUDA
  * events over about `ms` milliseconds. */
 int lmm_fp32_peak_tflops(int32_t device, double ms, double *tflops);
+/* The same for FP64 FMA (DFMA chains): the roofline of the FP64 kernels. */
+int lmm_fp64_peak_tflops(int32_t device, double ms, double *tflops);
 /* Measured special-function (MUFU) throughput on `device`, in 10^9 operations
  * per second, for ex2.approx, rcp.approx and the two alternating (the mix the
  * LMM cells issue: one exp and one reciprocal per cell), each from an
