@@ -254,8 +254,8 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     if (fam == 0)
         return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for nn=" + std::to_string(e->nn) +
                                              ", nmat=" + std::to_string(e->nmat));
-    if (fam == 2 && mode != Mode::Fused)
-        return fail(LMM_ERR_UNSUPPORTED, "the forward/backward pair covers nn=80, nmat=40 only");
+    if (philox && mode != Mode::Fused)
+        return fail(LMM_ERR_UNSUPPORTED, "the forward/backward pair reads its normals from memory");
     LMM_TRY(set_device(e));
     int bps = 0;
     LMM_TRY(blocks_per_sm(e, fam, mode, philox, &bps));
@@ -878,7 +878,11 @@ int lmm_tape_create(lmm_engine *e, int64_t paths, lmm_tape **out)
     std::unique_ptr<lmm_tape> t(new lmm_tape());
     t->e = e;
     t->paths = paths;
-    LMM_TRY(t->buf.ensure(sizeof(float) * (size_t)(e->nn + e->nmat) * e->nscen * (size_t)paths));
+    // The thread-per-path kernels (nn=80, nmat=40) keep the terminal rates and
+    // the per-step drift sums; the warp-per-path backward recomputes its
+    // forward from the same normals and needs no tape.
+    if (f32_family(e) == 1)
+        LMM_TRY(t->buf.ensure(sizeof(float) * (size_t)(e->nn + e->nmat) * e->nscen * (size_t)paths));
     *out = t.release();
     return LMM_OK;
 }

@@ -35,7 +35,7 @@ struct WppLay {
     size_t kc, l0, il0, ost, okf, okd, owf, owd, warp0, per_warp, ck, vg, lw, bw, acc, bytes;
 };
 
-__host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
+__host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S, Mode mode = Mode::Fused)
 {
     WppLay L{};
     L.nn = nn;
@@ -43,7 +43,7 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S)
     L.S = S;
     L.M = nn - nmat;
     L.nck = (nmat + kWppCkpt - 1) / kWppCkpt;
-    L.nout = 1 + 2 * nn;
+    L.nout = mode == Mode::Fused ? 1 + 2 * nn : (mode == Mode::Forward ? 1 : 2 * nn);
     size_t o = 0;
     L.kc = o; o = al16(o + 16 * (size_t)(nn + 1));    // [0]: zeros, [k+1]: constants of k
     L.l0 = o; o = al16(o + 4 * (size_t)nn);
@@ -199,13 +199,17 @@ struct ZChunk {
     }
 };
 
-template <int S, bool PHILOX>
+// MODE: Fused (value + all Greeks), Forward (value only) or Backward (Greeks
+// of vbar[scen] x value; the forward is recomputed from the same normals, so
+// no tape is needed).
+template <int S, bool PHILOX, Mode MODE>
 __global__ void __launch_bounds__(kWppBlock, 3)
-k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w)
+k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
+      const double *__restrict__ vbar)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nn = m.nn, nmat = m.nmat;
-    const WppLay Ly = wpp_layout(nn, nmat, S);
+    const WppLay Ly = wpp_layout(nn, nmat, S, MODE);
     const int M = Ly.M, nout = Ly.nout;
     float4 *kc_s = reinterpret_cast<float4 *>(smem + Ly.kc);
     float *l0_s = reinterpret_cast<float *>(smem + Ly.l0);
@@ -248,6 +252,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     }
 
     const float delta = m.delta, sqd = m.sqd, d2 = m.d2;
+    const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
     const int64_t ibase = (int64_t)item * w.ppt * kWppWarps;
     for (int j = 0; j < w.ppt; ++j) {
         const int64_t p = ibase + (int64_t)j * kWppWarps + warp;
@@ -266,7 +271,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         for (int n = 0; n < nmat; ++n) {
             if (n % kWppCkpt == 0) {
 #pragma unroll
-                for (int s = 0; s < S; ++s) ck_s[(n / kWppCkpt) * 32 * S + S * lane + s] = L[s];
+                for (int s = 0; s < S; ++s)
+                    if (MODE != Mode::Forward) ck_s[(n / kWppCkpt) * 32 * S + S * lane + s] = L[s];
             }
             const float sqez = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
             wpp_fwd_step<S>(L, base, n, sqez, lane, kc_s, delta, nullptr, nullptr);
@@ -300,11 +306,12 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 }
             }
             V = disc * vs;
+            if (MODE == Mode::Forward) mask = 0ull;     // no adjoint
             // :173-184 with the rate kept apart from its adjoint; lw_s[i] becomes
             // the log-adjoint of rate i >= nmat. B[m] comes from the forward
             // (bw_s): rebuilding it backwards from the last, smallest factor
             // would underflow FP32 on paths whose rates grow large.
-            const float scale = -(float)disc * delta;
+            const float scale = -vb * (float)disc * delta;
             float Sb = 0.0f, Bb = 0.0f;
             for (int mm = M - 1; mm >= 0; --mm) {
                 const float Ln = lw_s[nmat + mm];
@@ -323,7 +330,14 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         }
         V = __shfl_sync(0xffffffffu, V, 0);
         __syncwarp();
-        const float vsd = -(float)V * delta;
+        if (MODE == Mode::Forward) {
+            if (lane == 0) {
+                acc[0] += V;
+                acc[nout] += V * V;
+            }
+            continue;
+        }
+        const float vsd = -vb * (float)V * delta;
 #pragma unroll
         for (int s = 0; s < S; ++s) {
             const int i = S * lane + s;
@@ -351,7 +365,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         }
         // ---- accumulate this path: value, deltas, vegas ----
         __syncwarp();
-        if (lane == 0) {
+        constexpr int doff = MODE == Mode::Fused ? 1 : 0;   // deltas at doff, vegas at doff + nn
+        if (MODE == Mode::Fused && lane == 0) {
             acc[0] += V;
             acc[nout] += V * V;
         }
@@ -360,14 +375,14 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             const int i = S * lane + s;
             if (i < nn) {
                 const double dl = (double)(Pb[s] * il0_s[i]);
-                acc[1 + i] += dl;
-                acc[nout + 1 + i] += dl * dl;
+                acc[doff + i] += dl;
+                acc[nout + doff + i] += dl * dl;
             }
         }
         for (int k = lane; k < nn; k += 32) {
             const double vgk = (double)vg_s[k + 1];
-            acc[1 + nn + k] += vgk;
-            acc[nout + 1 + nn + k] += vgk * vgk;
+            acc[doff + nn + k] += vgk;
+            acc[nout + doff + nn + k] += vgk * vgk;
             vg_s[k + 1] = 0.0f;
         }
         __syncwarp();
@@ -381,27 +396,51 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     }
 }
 
-template <int S>
-int wpp_s_bytes(int nn, int nmat) { return (int)wpp_layout(nn, nmat, S).bytes; }
-
-template <int S, bool PHILOX>
+template <int S, bool PHILOX, Mode MODE>
 cudaError_t wpp_launch_s(const DevModel &m, const float *z, uint64_t seed, int64_t path0, const Work &w,
-                         cudaStream_t st)
+                         const double *vbar, cudaStream_t st)
 {
-    const int bytes = wpp_s_bytes<S>(m.nn, m.nmat);
-    cudaError_t e = cudaFuncSetAttribute(k_wpp<S, PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    const int bytes = (int)wpp_layout(m.nn, m.nmat, S, MODE).bytes;
+    auto kern = k_wpp<S, PHILOX, MODE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    k_wpp<S, PHILOX><<<(unsigned)((int64_t)m.nscen * w.items), kWppBlock, bytes, st>>>(m, z, seed, path0, w);
+    kern<<<(unsigned)((int64_t)m.nscen * w.items), kWppBlock, bytes, st>>>(m, z, seed, path0, w, vbar);
     return cudaGetLastError();
 }
 
-template <int S, bool PHILOX>
+template <int S, bool PHILOX, Mode MODE>
 cudaError_t wpp_occ_s(int nn, int nmat, int *blocks)
 {
-    const int bytes = wpp_s_bytes<S>(nn, nmat);
-    cudaError_t e = cudaFuncSetAttribute(k_wpp<S, PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    const int bytes = (int)wpp_layout(nn, nmat, S, MODE).bytes;
+    auto kern = k_wpp<S, PHILOX, MODE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_wpp<S, PHILOX>, kWppBlock, bytes);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, kWppBlock, bytes);
+}
+
+// The instantiated variants: Fused with normals from memory or Philox;
+// Forward and Backward (the ABI pair) with normals from memory.
+template <int S>
+cudaError_t wpp_dispatch_launch(const DevModel &m, Mode mode, bool philox, const float *z, uint64_t seed,
+                                int64_t path0, const Work &w, const double *vbar, cudaStream_t st)
+{
+    if (mode == Mode::Fused)
+        return philox ? wpp_launch_s<S, true, Mode::Fused>(m, z, seed, path0, w, vbar, st)
+                      : wpp_launch_s<S, false, Mode::Fused>(m, z, seed, path0, w, vbar, st);
+    if (philox) return cudaErrorNotSupported;
+    return mode == Mode::Forward ? wpp_launch_s<S, false, Mode::Forward>(m, z, seed, path0, w, vbar, st)
+                                 : wpp_launch_s<S, false, Mode::Backward>(m, z, seed, path0, w, vbar, st);
+}
+
+template <int S>
+cudaError_t wpp_dispatch_occ(int nn, int nmat, Mode mode, bool philox, int *blocks)
+{
+    if (mode == Mode::Fused)
+        return philox ? wpp_occ_s<S, true, Mode::Fused>(nn, nmat, blocks)
+                      : wpp_occ_s<S, false, Mode::Fused>(nn, nmat, blocks);
+    if (philox) return cudaErrorNotSupported;
+    return mode == Mode::Forward ? wpp_occ_s<S, false, Mode::Forward>(nn, nmat, blocks)
+                                 : wpp_occ_s<S, false, Mode::Backward>(nn, nmat, blocks);
 }
 
 // Slots per lane for a shape: the smallest instantiated S with 32*S >= nn.
@@ -427,26 +466,26 @@ int wpp_block_threads() { return kWppBlock; }
 cudaError_t wpp_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks)
 {
     *blocks = 0;
-    if (mode != Mode::Fused || !f32_wpp_supports(nn, nmat)) return cudaErrorNotSupported;
+    if (!f32_wpp_supports(nn, nmat)) return cudaErrorNotSupported;
     switch (wpp_slots(nn)) {
-        case 2: return philox ? wpp_occ_s<2, true>(nn, nmat, blocks) : wpp_occ_s<2, false>(nn, nmat, blocks);
-        case 3: return philox ? wpp_occ_s<3, true>(nn, nmat, blocks) : wpp_occ_s<3, false>(nn, nmat, blocks);
-        case 5: return philox ? wpp_occ_s<5, true>(nn, nmat, blocks) : wpp_occ_s<5, false>(nn, nmat, blocks);
-        case 8: return philox ? wpp_occ_s<8, true>(nn, nmat, blocks) : wpp_occ_s<8, false>(nn, nmat, blocks);
+        case 2: return wpp_dispatch_occ<2>(nn, nmat, mode, philox, blocks);
+        case 3: return wpp_dispatch_occ<3>(nn, nmat, mode, philox, blocks);
+        case 5: return wpp_dispatch_occ<5>(nn, nmat, mode, philox, blocks);
+        case 8: return wpp_dispatch_occ<8>(nn, nmat, mode, philox, blocks);
     }
     return cudaErrorNotSupported;
 }
 
 cudaError_t launch_wpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
-                           int64_t path0, bool philox, const Work &w, float *, const double *,
+                           int64_t path0, bool philox, const Work &w, float *, const double *vbar,
                            cudaStream_t s)
 {
-    if (mode != Mode::Fused || !f32_wpp_supports(m.nn, m.nmat)) return cudaErrorNotSupported;
+    if (!f32_wpp_supports(m.nn, m.nmat)) return cudaErrorNotSupported;
     switch (wpp_slots(m.nn)) {
-        case 2: return philox ? wpp_launch_s<2, true>(m, z, seed, path0, w, s) : wpp_launch_s<2, false>(m, z, seed, path0, w, s);
-        case 3: return philox ? wpp_launch_s<3, true>(m, z, seed, path0, w, s) : wpp_launch_s<3, false>(m, z, seed, path0, w, s);
-        case 5: return philox ? wpp_launch_s<5, true>(m, z, seed, path0, w, s) : wpp_launch_s<5, false>(m, z, seed, path0, w, s);
-        case 8: return philox ? wpp_launch_s<8, true>(m, z, seed, path0, w, s) : wpp_launch_s<8, false>(m, z, seed, path0, w, s);
+        case 2: return wpp_dispatch_launch<2>(m, mode, philox, z, seed, path0, w, vbar, s);
+        case 3: return wpp_dispatch_launch<3>(m, mode, philox, z, seed, path0, w, vbar, s);
+        case 5: return wpp_dispatch_launch<5>(m, mode, philox, z, seed, path0, w, vbar, s);
+        case 8: return wpp_dispatch_launch<8>(m, mode, philox, z, seed, path0, w, vbar, s);
     }
     return cudaErrorNotSupported;
 }

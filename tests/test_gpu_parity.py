@@ -285,16 +285,40 @@ def test_other_shapes_fp32_match_oracle(P, nn, nmat, nopt):
     assert_f32_close(g[0], m, cfg.nn, f"{nn}x{nmat}")
 
 
-def test_pair_api_limited_to_reference_shape(P):
+@pytest.mark.parametrize("shape", [(160, 120, 3), (33, 7, 2), (200, 100, 4)])
+def test_pair_api_on_warp_per_path_shapes(P, shape):
+    """For shapes other than 80x40 the backward recomputes the forward from the
+    same normals: value and vbar-scaled Greeks equal the fused call's."""
+    import torch
+    nn, nmat, seed = shape
+    cfg = cfgs().workload(3, 256) if nn == 160 else _random_cfg(nn, nmat, 6, seed, 256)
+    z = O.normals_f32(40 + nn, cfg.paths, cfg.nmat)
+    dz = torch.from_numpy(z).cuda()
+    with P.Engine(cfg) as e:
+        fused, _ = e.greeks_f32(z)
+        t = e.tape(cfg.paths)
+        val = torch.zeros(1, dtype=torch.float64, device="cuda")
+        grad = torch.zeros(2 * cfg.nn, dtype=torch.float64, device="cuda")
+        e.forward_f32_device(dz.data_ptr(), cfg.paths, t, val.data_ptr())
+        e.backward_f32_device(dz.data_ptr(), t, [-1.5], grad.data_ptr())
+        e.synchronize()
+        t.close()
+    f = fused[0]
+    assert val.item() == pytest.approx(f[0], rel=1e-12)
+    np.testing.assert_allclose(grad.cpu().numpy(), -1.5 * f[1:], rtol=2e-6, atol=1e-6 * np.abs(f[1:]).max())
+
+
+def test_pair_api_needs_normals(P):
+    """The pair reads its normals from memory: a NULL normals pointer is an
+    argument error, for every shape."""
     import torch
     cfg = cfgs().workload(3, 64)
-    dz = torch.zeros(64 * cfg.nmat, dtype=torch.float32, device="cuda")
     val = torch.zeros(1, dtype=torch.float64, device="cuda")
     with P.Engine(cfg) as e:
         t = e.tape(64)
         with pytest.raises(P.LmmError) as ei:
-            e.forward_f32_device(dz.data_ptr(), 64, t, val.data_ptr())
-        assert ei.value.code == -2
+            e.forward_f32_device(0, 64, t, val.data_ptr())
+        assert ei.value.code == -1
         t.close()
 
 
