@@ -100,6 +100,7 @@ struct lmm_engine {
     float *wf_rows = nullptr;      // [1+nopt][nopt] weights: row 0 the caller's, row 1+g unit at g
     double *wd_rows = nullptr;
     DevBuf partial, z32, z64, out, se, flag, vbar;
+    DevBuf wscratch;               // warp-per-path kernels: Y_top per warp, step and lane
     std::map<int, int> bps;        // cached blocks per SM per kernel variant
     int32_t last_launches = 0;
     bool timing = false;
@@ -243,6 +244,16 @@ int check_paths(int64_t paths)
     return LMM_OK;
 }
 
+// Scratch of the warp-per-path kernels for a grid of `blocks` blocks (the
+// forward's per-step drift sums at each lane's top rate, and rate checkpoints).
+int wpp_scratch(lmm_engine *e, int64_t blocks, float **out)
+{
+    const size_t warps = (size_t)blocks * (lmm::wpp_block_threads() / 32);
+    LMM_TRY(e->wscratch.ensure(sizeof(float) * warps * lmm::wpp_scratch_floats_per_warp(e->nn, e->nmat)));
+    *out = e->wscratch.as<float>();
+    return LMM_OK;
+}
+
 int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t path0, bool philox,
             int64_t paths, float *tape, const double *d_vbar, double *d_mean, double *d_se)
 {
@@ -265,6 +276,7 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     const int per_batch = fam == 1 ? block : block / 32;
     Work w{};
     LMM_TRY(plan(e, e->nscen, paths, per_batch, bps, nout, &w));
+    if (fam == 2) LMM_TRY(wpp_scratch(e, (int64_t)e->nscen * w.items, &tape));
     LMM_TRY(e->flag.ensure(sizeof(int)));
     LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
     mark(e, 0);
@@ -525,6 +537,7 @@ int lmm_engine_destroy(lmm_engine *e)
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->model.release();
+    e->wscratch.release();
     e->partial.release();
     e->z32.release();
     e->z64.release();
@@ -790,6 +803,12 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
         total_items += citems[c];
     }
     LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)total_items * 2 * nout));
+    float *wscr = nullptr;
+    if (fam == 2) {
+        int64_t most = 0;
+        for (int c = 0; c < C; ++c) most = std::max(most, citems[c]);
+        LMM_TRY(wpp_scratch(e, most, &wscr));     // the pieces run one after another
+    }
     LMM_TRY(e->flag.ensure(sizeof(int)));
     if (!e->copy_stream) LMM_CK(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));
     if (!e->ready_ev) LMM_CK(cudaEventCreateWithFlags(&e->ready_ev, cudaEventDisableTiming));
@@ -818,7 +837,7 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
         const float *zc = dz + (size_t)cfirst[c] * e->nmat;
         cudaError_t err = fam == 1
                               ? lmm::launch_tpp_any(e->dm, Mode::Fused, zc, 0, 0, false, w, nullptr, nullptr, e->stream)
-                              : lmm::launch_wpp_any(e->dm, Mode::Fused, zc, 0, 0, false, w, nullptr, nullptr, e->stream);
+                              : lmm::launch_wpp_any(e->dm, Mode::Fused, zc, 0, 0, false, w, wscr, nullptr, e->stream);
         if (err != cudaSuccess) return cuda_fail(err, "FP32 LMM kernel launch");
         part += (size_t)citems[c] * 2 * nout;
     }

@@ -1,5 +1,5 @@
 // FP32 warp-per-path LMM kernels: any NN <= 256 (long tenor, e.g. NN=160,
-// NMAT=120), reverse sweep recomputed from checkpoints.
+// NMAT=120).
 //
 // One warp carries one Monte Carlo path. Lane l holds the S consecutive rates
 // i = S*l + s (s < S) in registers, so
@@ -8,13 +8,18 @@
 //     plus an exclusive warp scan of the lane totals (shuffles);
 //   - the reverse running sum v1 of path_calc_b2 (:108), a suffix sum over i,
 //     is the mirror image (local suffix + exclusive warp suffix scan).
-// The forward stores the rates every kWppCkpt steps in shared memory. The
-// reverse sweep restores each checkpoint, recomputes its kWppCkpt steps
-// keeping the pre-step rates and the drift sums of every cell in registers,
-// then runs the adjoint of those steps backwards (Pb = L dV/dL, the
-// log-adjoint):
+// Reverse sweep without a stored trajectory: the forward saves, per step and
+// lane, Y_top = V + sqrt(delta) z at the lane's top rate (one float per lane
+// and step, in a per-warp device scratch that stays in L2), and the rates
+// every kWppReset steps. The reverse restarts each step from Y_top and runs
+// the Euler step backwards down the lane's own slots,
+//   L_{n,i} = L_{n+1,i} 2^-(a_k Y_i + c_k),  Y_{i-1} = Y_i - delta^2 lambda_k t_i,
+// so the serial chain is S cells long, not NN; at every kWppReset-th step it
+// replaces the rebuilt rates by the saved ones, so FP32 rounding of the
+// reconstruction accumulates over at most kWppReset steps. The adjoint in log form
+// (Pb = L dV/dL) is
 //   S_i = sum_{j>=i} lambda_k Pb_j,  Pb_i += delta^2 lambda_k t r S_i
-//   dV/dlambda_k += Pb_i (V_i + sqez - delta lambda_k) + delta^2 t S_i.
+//   dV/dlambda_k += Pb_i (Y_i - delta lambda_k) + delta^2 t S_i.
 // The payoff (portfolio_b :120-211, aliasing fixed) runs with FP64 products:
 // the discount product is a warp product reduction, the annuity recursion
 // runs on lane 0.
@@ -25,14 +30,32 @@ namespace {
 
 constexpr int kWppBlock = 128;
 constexpr int kWppWarps = kWppBlock / 32;
-constexpr int kWppCkpt = 8;
+#ifndef LMM_WPP_RESET
+#define LMM_WPP_RESET 8
+#endif
+constexpr int kWppReset = LMM_WPP_RESET;   // the reverse restores the exact rates every kWppReset steps
+
+// Resident blocks the register budget is sized for: 6 (shared memory allows
+// no more at NN=160); 5 for S=8, which spills at 6.
+#ifdef LMM_WPP_MINB
+__host__ __device__ constexpr int wpp_min_blocks(int) { return LMM_WPP_MINB; }
+#else
+__host__ __device__ constexpr int wpp_min_blocks(int S) { return S >= 8 ? 5 : 6; }
+#endif
+
+// Scratch per warp, in floats: Y_top per step and lane, then the rates at
+// every kWppReset-th step, [checkpoint][slot][lane].
+__host__ __device__ constexpr size_t wpp_scratch_floats(int nmat, int S)
+{
+    return (size_t)32 * nmat + (size_t)32 * S * ((nmat + kWppReset - 1) / kWppReset);
+}
 
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 
 // Shared-memory layout (bytes), shared by host and device.
 struct WppLay {
-    int nn, nmat, S, nck, nout, M;
-    size_t kc, l0, il0, ost, okf, okd, owf, owd, warp0, per_warp, ck, vg, lw, bw, acc, bytes;
+    int nn, nmat, S, nout, M;
+    size_t kc, l0, il0, ost, okf, okd, owf, owd, warp0, per_warp, vg, lw, bw, acc, bytes;
 };
 
 __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S, Mode mode = Mode::Fused)
@@ -42,7 +65,6 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S, Mode mode 
     L.nmat = nmat;
     L.S = S;
     L.M = nn - nmat;
-    L.nck = (nmat + kWppCkpt - 1) / kWppCkpt;
     L.nout = mode == Mode::Fused ? 1 + 2 * nn : (mode == Mode::Forward ? 1 : 2 * nn);
     size_t o = 0;
     L.kc = o; o = al16(o + 16 * (size_t)(nn + 1));    // [0]: zeros, [k+1]: constants of k
@@ -55,7 +77,6 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S, Mode mode 
     L.owd = o; o = al16(o + 8 * (size_t)kMaxNopt);
     L.warp0 = o;
     size_t w = 0;
-    L.ck = w; w = al16(w + 4 * (size_t)L.nck * 32 * S);   // checkpoints [nck][32*S]
     L.vg = w; w = al16(w + 4 * (size_t)(32 * S + 1));     // vegas [1+32*S] (row k+1; row 0 discards)
     L.lw = w; w = al16(w + 4 * (size_t)32 * S);           // payoff staging [32*S]
     L.bw = w; w = al16(w + 4 * (size_t)32 * S);           // annuity factors B[m] [32*S]
@@ -104,14 +125,11 @@ __device__ __forceinline__ int wpp_row(const int (&base)[S], int s, int n)
     return max(base[s] - n, 0);
 }
 
-// One forward step n over the lane's slots. If T/Vs are given, the cell's
-// pre-step rate and its drift sum plus sqrt(delta) z are kept (for the
-// recompute of a checkpoint segment). The rate, not t = L/(1+delta L), is
-// kept: forming r = 1/(1+delta L) again as 1 - delta t would cancel
-// catastrophically on paths whose rates grow large.
+// One forward step n over the lane's slots; returns Y at the lane's top slot
+// (its drift sum plus sqrt(delta) z), from which the reverse restarts.
 template <int S>
-__device__ __forceinline__ void wpp_fwd_step(float (&L)[S], const int (&base)[S], int n, float sqez,
-                                             int lane, const float4 *kc, float delta, float *T, float *Vs)
+__device__ __forceinline__ float wpp_fwd_step(float (&L)[S], const int (&base)[S], int n, float sqez,
+                                              int lane, const float4 *kc, float delta)
 {
     float a[S];
     float4 kk[S];
@@ -125,21 +143,17 @@ __device__ __forceinline__ void wpp_fwd_step(float (&L)[S], const int (&base)[S]
     }
     const float X = warp_excl_prefix(P, lane) + sqez;
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const float Y = X + a[s];                   // V_i + sqrt(delta) z
-        if (T) {
-            T[s] = L[s];
-            Vs[s] = Y;
-        }
-        L[s] *= ex2_approx(fmaf(kk[s].x, Y, kk[s].y));
-    }
+    for (int s = 0; s < S; ++s) L[s] *= ex2_approx(fmaf(kk[s].x, X + a[s], kk[s].y));
+    return X + a[S - 1];
 }
 
-// Adjoint of step n (path_calc_b2 :100-112 in log-adjoint form) + vega.
+// Reverse step n (path_calc_b2 :100-112 in log-adjoint form) + vega: L holds
+// L_{n+1} on entry and L_n on exit; ytop is the forward's Y at the lane's top
+// slot. The suffix sum takes the log-adjoints before the step's update.
 template <int S>
-__device__ __forceinline__ void wpp_rev_step(float (&Pb)[S], const int (&base)[S], int n, int lane,
-                                             const float4 *kc, float *vg, const float *T, const float *Vs,
-                                             float delta, float d2)
+__device__ __forceinline__ void wpp_rev_step(float (&L)[S], float (&Pb)[S], const int (&base)[S], int n,
+                                             int lane, float ytop, const float4 *kc, float *vg, float delta,
+                                             float d2)
 {
     float b[S];
     float4 kk[S];
@@ -150,15 +164,18 @@ __device__ __forceinline__ void wpp_rev_step(float (&Pb)[S], const int (&base)[S
         Q = fmaf(kk[s].w, Pb[s], Q);
         b[s] = Q;                                   // local inclusive suffix
     }
-    const float Y = warp_excl_suffix(Q, lane);
+    const float Yx = warp_excl_suffix(Q, lane);
+    float Y = ytop;
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const float Ssum = Y + b[s];
-        const float r = rcp_approx(fmaf(delta, T[s], 1.0f));
-        const float t = T[s] * r;
-        const float tS = t * Ssum;
-        vg[wpp_row(base, s, n)] += fmaf(Pb[s], fmaf(-delta, kk[s].w, Vs[s]), d2 * tS);
+    for (int s = S - 1; s >= 0; --s) {
+        const float Ln = L[s] * ex2_approx(-fmaf(kk[s].x, Y, kk[s].y));
+        const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
+        const float t = Ln * r;
+        const float tS = t * (Yx + b[s]);
+        vg[wpp_row(base, s, n)] += fmaf(Pb[s], fmaf(-delta, kk[s].w, Y), d2 * tS);
         Pb[s] = fmaf(kk[s].z * r, tS, Pb[s]);
+        L[s] = Ln;
+        Y = fmaf(-kk[s].z, t, Y);
     }
     // The next step's vega rows overlap neighbouring lanes' rows of this
     // step: order the shared-memory read-modify-writes across the warp.
@@ -201,11 +218,13 @@ struct ZChunk {
 
 // MODE: Fused (value + all Greeks), Forward (value only) or Backward (Greeks
 // of vbar[scen] x value; the forward is recomputed from the same normals, so
-// no tape is needed).
+// no tape is needed). ytop: gridDim.x * kWppWarps blocks of
+// wpp_scratch_floats(nmat, S) floats of scratch, one per warp (unused in
+// Forward mode).
 template <int S, bool PHILOX, Mode MODE>
-__global__ void __launch_bounds__(kWppBlock, 3)
+__global__ void __launch_bounds__(kWppBlock, wpp_min_blocks(S))
 k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
-      const double *__restrict__ vbar)
+      const double *__restrict__ vbar, float *__restrict__ ytop)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nn = m.nn, nmat = m.nmat;
@@ -221,7 +240,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     double *owd_s = reinterpret_cast<double *>(smem + Ly.owd);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned char *wbase = smem + Ly.warp0 + warp * Ly.per_warp;
-    float *ck_s = reinterpret_cast<float *>(wbase + Ly.ck);
+    float *yt = ytop + ((size_t)blockIdx.x * kWppWarps + warp) * wpp_scratch_floats(nmat, S) + lane;
+    float *ck = yt + (size_t)32 * nmat;     // ck[(c*S + s)*32]: rate of slot s at step c*kWppReset
     float *vg_s = reinterpret_cast<float *>(wbase + Ly.vg);
     float *lw_s = reinterpret_cast<float *>(wbase + Ly.lw);
     float *bw_s = reinterpret_cast<float *>(wbase + Ly.bw);
@@ -267,15 +287,15 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             const int i = S * lane + s;
             L[s] = i < nn ? l0_s[i] : 1.0f;
         }
-        // ---- forward with checkpoints ----
+        // ---- forward ----
         for (int n = 0; n < nmat; ++n) {
-            if (n % kWppCkpt == 0) {
+            if (MODE != Mode::Forward && n % kWppReset == 0) {
 #pragma unroll
-                for (int s = 0; s < S; ++s)
-                    if (MODE != Mode::Forward) ck_s[(n / kWppCkpt) * 32 * S + S * lane + s] = L[s];
+                for (int s = 0; s < S; ++s) ck[((n / kWppReset) * S + s) * 32] = L[s];
             }
             const float sqez = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
-            wpp_fwd_step<S>(L, base, n, sqez, lane, kc_s, delta, nullptr, nullptr);
+            const float y = wpp_fwd_step<S>(L, base, n, sqez, lane, kc_s, delta);
+            if (MODE != Mode::Forward) yt[n * 32] = y;
         }
         // ---- payoff (FP64 products) and its adjoint ----
         double dprod = 1.0;
@@ -344,23 +364,15 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             if (i < nmat) Pb[s] = vsd * (L[s] * __frcp_rn(fmaf(delta, L[s], 1.0f)));
             else Pb[s] = i < nn ? lw_s[i] : 0.0f;
         }
-        // ---- reverse, one checkpoint segment at a time ----
-        for (int c = Ly.nck - 1; c >= 0; --c) {
+        // ---- reverse: each step rebuilt from the forward's Y_top ----
+        float ynext = yt[(nmat - 1) * 32];
+        for (int n = nmat - 1; n >= 0; --n) {
+            const float y = ynext;
+            if (n > 0) ynext = yt[(n - 1) * 32];
+            wpp_rev_step<S>(L, Pb, base, n, lane, y, kc_s, vg_s, delta, d2);
+            if (n % kWppReset == 0) {
 #pragma unroll
-            for (int s = 0; s < S; ++s) L[s] = ck_s[c * 32 * S + S * lane + s];
-            float T[kWppCkpt][S], Vs[kWppCkpt][S], zs[kWppCkpt];
-#pragma unroll
-            for (int jj = 0; jj < kWppCkpt; ++jj) {
-                const int n = c * kWppCkpt + jj;
-                if (n < nmat) {
-                    zs[jj] = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
-                    wpp_fwd_step<S>(L, base, n, zs[jj], lane, kc_s, delta, T[jj], Vs[jj]);
-                }
-            }
-#pragma unroll
-            for (int jj = kWppCkpt - 1; jj >= 0; --jj) {
-                const int n = c * kWppCkpt + jj;
-                if (n < nmat) wpp_rev_step<S>(Pb, base, n, lane, kc_s, vg_s, T[jj], Vs[jj], delta, d2);
+                for (int s = 0; s < S; ++s) L[s] = ck[((n / kWppReset) * S + s) * 32];
             }
         }
         // ---- accumulate this path: value, deltas, vegas ----
@@ -398,13 +410,13 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 
 template <int S, bool PHILOX, Mode MODE>
 cudaError_t wpp_launch_s(const DevModel &m, const float *z, uint64_t seed, int64_t path0, const Work &w,
-                         const double *vbar, cudaStream_t st)
+                         const double *vbar, float *ytop, cudaStream_t st)
 {
     const int bytes = (int)wpp_layout(m.nn, m.nmat, S, MODE).bytes;
     auto kern = k_wpp<S, PHILOX, MODE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    kern<<<(unsigned)((int64_t)m.nscen * w.items), kWppBlock, bytes, st>>>(m, z, seed, path0, w, vbar);
+    kern<<<(unsigned)((int64_t)m.nscen * w.items), kWppBlock, bytes, st>>>(m, z, seed, path0, w, vbar, ytop);
     return cudaGetLastError();
 }
 
@@ -422,14 +434,15 @@ cudaError_t wpp_occ_s(int nn, int nmat, int *blocks)
 // Forward and Backward (the ABI pair) with normals from memory.
 template <int S>
 cudaError_t wpp_dispatch_launch(const DevModel &m, Mode mode, bool philox, const float *z, uint64_t seed,
-                                int64_t path0, const Work &w, const double *vbar, cudaStream_t st)
+                                int64_t path0, const Work &w, const double *vbar, float *ytop,
+                                cudaStream_t st)
 {
     if (mode == Mode::Fused)
-        return philox ? wpp_launch_s<S, true, Mode::Fused>(m, z, seed, path0, w, vbar, st)
-                      : wpp_launch_s<S, false, Mode::Fused>(m, z, seed, path0, w, vbar, st);
+        return philox ? wpp_launch_s<S, true, Mode::Fused>(m, z, seed, path0, w, vbar, ytop, st)
+                      : wpp_launch_s<S, false, Mode::Fused>(m, z, seed, path0, w, vbar, ytop, st);
     if (philox) return cudaErrorNotSupported;
-    return mode == Mode::Forward ? wpp_launch_s<S, false, Mode::Forward>(m, z, seed, path0, w, vbar, st)
-                                 : wpp_launch_s<S, false, Mode::Backward>(m, z, seed, path0, w, vbar, st);
+    return mode == Mode::Forward ? wpp_launch_s<S, false, Mode::Forward>(m, z, seed, path0, w, vbar, ytop, st)
+                                 : wpp_launch_s<S, false, Mode::Backward>(m, z, seed, path0, w, vbar, ytop, st);
 }
 
 template <int S>
@@ -443,6 +456,8 @@ cudaError_t wpp_dispatch_occ(int nn, int nmat, Mode mode, bool philox, int *bloc
                                  : wpp_occ_s<S, false, Mode::Backward>(nn, nmat, blocks);
 }
 
+}  // namespace
+
 // Slots per lane for a shape: the smallest instantiated S with 32*S >= nn.
 int wpp_slots(int nn)
 {
@@ -453,7 +468,7 @@ int wpp_slots(int nn)
     return 0;
 }
 
-}  // namespace
+size_t wpp_scratch_floats_per_warp(int nn, int nmat) { return wpp_scratch_floats(nmat, wpp_slots(nn)); }
 
 bool f32_wpp_supports(int nn, int nmat)
 {
@@ -477,15 +492,16 @@ cudaError_t wpp_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blo
 }
 
 cudaError_t launch_wpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
-                           int64_t path0, bool philox, const Work &w, float *, const double *vbar,
+                           int64_t path0, bool philox, const Work &w, float *ytop, const double *vbar,
                            cudaStream_t s)
 {
     if (!f32_wpp_supports(m.nn, m.nmat)) return cudaErrorNotSupported;
+    if (mode != Mode::Forward && !ytop) return cudaErrorInvalidValue;
     switch (wpp_slots(m.nn)) {
-        case 2: return wpp_dispatch_launch<2>(m, mode, philox, z, seed, path0, w, vbar, s);
-        case 3: return wpp_dispatch_launch<3>(m, mode, philox, z, seed, path0, w, vbar, s);
-        case 5: return wpp_dispatch_launch<5>(m, mode, philox, z, seed, path0, w, vbar, s);
-        case 8: return wpp_dispatch_launch<8>(m, mode, philox, z, seed, path0, w, vbar, s);
+        case 2: return wpp_dispatch_launch<2>(m, mode, philox, z, seed, path0, w, vbar, ytop, s);
+        case 3: return wpp_dispatch_launch<3>(m, mode, philox, z, seed, path0, w, vbar, ytop, s);
+        case 5: return wpp_dispatch_launch<5>(m, mode, philox, z, seed, path0, w, vbar, ytop, s);
+        case 8: return wpp_dispatch_launch<8>(m, mode, philox, z, seed, path0, w, vbar, ytop, s);
     }
     return cudaErrorNotSupported;
 }

@@ -58,6 +58,10 @@ cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_
 bool f32_wpp_supports(int nn, int nmat);
 int wpp_block_threads();
 cudaError_t wpp_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks);
+// Device scratch the warp-per-path kernels take per warp (floats): the
+// forward's per-step drift sums at each lane's top rate, and rate checkpoints.
+size_t wpp_scratch_floats_per_warp(int nn, int nmat);
+int wpp_slots(int nn);
 cudaError_t launch_wpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
                            int64_t path0, bool philox, const Work &w, float *tape,
                            const double *vbar, cudaStream_t s);
