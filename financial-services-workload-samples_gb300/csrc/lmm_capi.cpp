@@ -435,11 +435,10 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
     const double d = p->delta;
     const double log2e = 1.4426950408889634073599246810019;
     std::vector<float4> kc(nn);
-    std::vector<float> kd(nn), L0f((size_t)ns * nn), iL0f((size_t)ns * nn);
+    std::vector<float> L0f((size_t)ns * nn), iL0f((size_t)ns * nn);
     for (int k = 0; k < nn; ++k) {
         const double l = p->lambda[k];
         kc[k] = make_float4((float)(l * log2e), (float)(-0.5 * d * l * l * log2e), (float)(d * d * l), (float)l);
-        kd[k] = (float)(d * l);
     }
     for (size_t i = 0; i < (size_t)ns * nn; ++i) {
         L0f[i] = (float)p->L0[i];
@@ -467,7 +466,7 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
         off += (bytes + 255) & ~size_t(255);
         return o;
     };
-    const size_t o_kc = sect(sizeof(float4) * nn), o_kd = sect(sizeof(float) * nn);
+    const size_t o_kc = sect(sizeof(float4) * nn);
     const size_t o_l0f = sect(sizeof(float) * L0f.size()), o_il0f = sect(sizeof(float) * iL0f.size());
     const size_t o_l0d = sect(sizeof(double) * L0f.size()), o_lamd = sect(sizeof(double) * nn);
     const size_t o_ost = sect(sizeof(int) * (M + 1)), o_okf = sect(sizeof(float) * std::max(1, nopt));
@@ -490,7 +489,6 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
         return bytes ? cudaMemcpy(base + o, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
     };
     LMM_CK(up(o_kc, kc.data(), sizeof(float4) * nn));
-    LMM_CK(up(o_kd, kd.data(), sizeof(float) * nn));
     LMM_CK(up(o_l0f, L0f.data(), sizeof(float) * L0f.size()));
     LMM_CK(up(o_il0f, iL0f.data(), sizeof(float) * iL0f.size()));
     LMM_CK(up(o_l0d, p->L0, sizeof(double) * L0f.size()));
@@ -514,7 +512,6 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
     m.deltad = d;
     m.sqdd = std::sqrt(d);
     m.kc = reinterpret_cast<const float4 *>(base + o_kc);
-    m.kd = reinterpret_cast<const float *>(base + o_kd);
     m.L0f = reinterpret_cast<const float *>(base + o_l0f);
     m.invL0f = reinterpret_cast<const float *>(base + o_il0f);
     m.L0d = reinterpret_cast<const double *>(base + o_l0d);

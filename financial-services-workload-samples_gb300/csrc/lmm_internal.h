@@ -13,7 +13,6 @@ constexpr int kMaxNopt = 64;
 // Per-engine model data resident in HBM, passed to kernels by value.
 // Per time-to-maturity k (the reference's lambda[i-n-1] index):
 //   kc[k] = { lambda_k*log2(e), -delta*lambda_k^2*log2(e)/2, delta^2*lambda_k, lambda_k }
-//   kd[k] = delta*lambda_k
 // so that one Euler cell (liborSwaptionGreeks.cpp:68-73) is
 //   t = L/(1+delta L); V += kc.z*t; L *= 2^(kc.x*(V + sqrt(delta) z) + kc.y)
 // with V = delta * (the reference's running sum v).
@@ -22,7 +21,6 @@ struct DevModel {
     float delta, sqd, d2;                 // delta, sqrt(delta), delta^2
     double deltad, sqdd;
     const float4 *kc;                     // [nn]
-    const float *kd;                      // [nn]
     const float *L0f;                     // [nscen][nn]
     const float *invL0f;                  // [nscen][nn]
     const double *L0d;                    // [nscen][nn]
@@ -53,8 +51,9 @@ cudaError_t tpp_blocks_per_sm(Mode mode, bool philox, int *blocks);
 cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
                            int64_t path0, bool philox, const Work &w, float *tape,
                            const double *vbar, cudaStream_t s);
-// FP32 warp-per-path kernels (lmm_f32_wpp.cu, any NN <= kMaxNN, reverse sweep
-// recomputed from checkpoints every kWppCkpt steps).
+// FP32 warp-per-path kernels (lmm_f32_wpp.cu, any NN <= kMaxNN; the reverse
+// sweep rebuilds each step from the forward's per-lane drift sums and takes
+// the saved rates every 8 steps).
 bool f32_wpp_supports(int nn, int nmat);
 int wpp_block_threads();
 cudaError_t wpp_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks);

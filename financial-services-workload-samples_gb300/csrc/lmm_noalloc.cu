@@ -34,7 +34,6 @@ constexpr int kMaxDevices = 64;
 // Model section of the scratch, uploaded by every call (device layout).
 struct NoallocModel {
     float4 kc[kNN];
-    float kd[kNN];
     float L0f[LMM_NOALLOC_MAX_SCEN * kNN];
     float iL0f[LMM_NOALLOC_MAX_SCEN * kNN];
     double L0d[LMM_NOALLOC_MAX_SCEN * kNN];
@@ -108,7 +107,6 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
     for (int k = 0; k < kNN; ++k) {
         const double l = p->lambda[k];
         hm.kc[k] = make_float4((float)(l * log2e), (float)(-0.5 * d * l * l * log2e), (float)(d * d * l), (float)l);
-        hm.kd[k] = (float)(d * l);
         hm.lamd[k] = l;
     }
     for (int i = 0; i < p->nscen * kNN; ++i) {
@@ -147,7 +145,6 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
     m.deltad = d;
     m.sqdd = std::sqrt(d);
     m.kc = dmod->kc;
-    m.kd = dmod->kd;
     m.L0f = dmod->L0f;
     m.invL0f = dmod->iL0f;
     m.L0d = dmod->L0d;

@@ -261,8 +261,9 @@ def _random_cfg(nn, nmat, nopt, seed, paths, vol=(0.1, 0.2)):
 
 @pytest.mark.parametrize("philox", [False, True])
 def test_long_tenor_checkpointed_fp32_matches_oracle(P, philox):
-    """Workload 3 (NN=160, NMAT=120, 30 swaptions): warp-per-path kernel with the
-    reverse sweep recomputed from checkpoints every 8 steps."""
+    """Workload 3 (NN=160, NMAT=120, 30 swaptions): warp-per-path kernel, whose
+    reverse sweep rebuilds each step from the forward's per-lane drift sums and
+    takes the rates saved every 8 steps."""
     cfg = cfgs().workload(3, 512)
     seed = 303
     z = O.normals_f32(seed, cfg.paths, cfg.nmat)
@@ -363,8 +364,8 @@ def test_pipelined_host_call_equals_device_call(P):
 
 
 def test_full_size_long_tenor_fp32_vs_fp64(P):
-    """Workload 3 at its named size (1,048,576 paths, NN=160, NMAT=120,
-    checkpoints every 8 steps) against the FP64 kernel on identical normals."""
+    """Workload 3 at its named size (1,048,576 paths, NN=160, NMAT=120, rates
+    saved every 8 steps) against the FP64 kernel on identical normals."""
     import torch
     cfg = cfgs().workload(3)
     n = cfg.paths
