@@ -163,7 +163,13 @@ def cpu_baseline_port(cfg, target_s=3.0, threads=0):
     t0 = time.perf_counter()
     O.reference_work(cfg, z, n, threads)
     dt = time.perf_counter() - t0
+    # the same on one core, on a sample sized for about a tenth of the time
+    n1 = max(16, int(n / max(threads, 1) / 10) // 16 * 16)
+    t1 = time.perf_counter()
+    O.reference_work(cfg, z, n1, 1)
+    dt1 = time.perf_counter() - t1
     return {"value": n / dt, "unit": "paths/s", "cores": threads, "kind": "port",
+            "value_1core": n1 / dt1,
             "sample": f"{n} paths of the same workload (FP64, value + {cfg.nn} deltas by the reference's "
                       f"adjoint; the reference computes no vegas), {dt:.2f} s wall on {threads} threads",
             "seconds": dt}
