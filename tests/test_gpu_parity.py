@@ -402,3 +402,32 @@ def test_full_size_scenario_sweep_consistent(P):
             e1.synchronize()
         r = one.cpu().numpy()
         np.testing.assert_allclose(g[s], r, rtol=1e-9, atol=1e-12 * np.abs(r).max())
+
+
+@pytest.mark.parametrize("nn,nmat,nopt", [(80, 40, 64), (96, 60, 64), (2, 1, 1), (3, 2, 2)])
+def test_portfolio_and_shape_limits(P, nn, nmat, nopt):
+    """The largest portfolio (64 swaptions: every bit of the payoff mask) on both
+    FP32 kernel families, and the smallest shapes (NN=2, NMAT=1)."""
+    cfg = _random_cfg(nn, nmat, nopt, 7000 + nn + nopt, 600)
+    z = O.normals_f32(nn + nopt, cfg.paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        g, _ = e.greeks_f32(z)
+        g64, _ = e.greeks_f64(z.astype(np.float64))
+    m, _ = O.greeks(cfg, z.astype(np.float64))
+    np.testing.assert_allclose(g64[0], m, rtol=1e-11, atol=1e-12 * np.abs(m).max())
+    if np.abs(m).max() > 0:
+        assert_f32_close(g[0], m, cfg.nn, f"{nn}x{nmat}, {nopt} swaptions")
+    else:                                   # out of the money on every path
+        assert np.all(g[0] == 0.0)
+
+
+@pytest.mark.parametrize("nn,nmat", [(80, 40), (160, 120)])
+def test_empty_portfolio_prices_zero(P, nn, nmat):
+    """No swaptions: value and every Greek are exactly 0 (FP32 and FP64)."""
+    cfg = cfgs().LmmConfig("empty", nn, nmat, 0.25, np.full(nn, 0.05), np.full(nn, 0.2),
+                           np.zeros(0, dtype=np.int32), np.zeros(0), 300)
+    z = O.normals_f32(5, cfg.paths, cfg.nmat)
+    with P.Engine(cfg) as e:
+        g, gse = e.greeks_f32(z)
+        g64, _ = e.greeks_f64(z.astype(np.float64))
+    assert np.all(g == 0.0) and np.all(gse == 0.0) and np.all(g64 == 0.0)
