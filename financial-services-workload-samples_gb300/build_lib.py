@@ -83,6 +83,29 @@ def build(force: bool = False, jobs: int | None = None, extra=(), verbose: bool 
     return LIB
 
 
+SHIM = os.path.join(PKG, "shim", "liborSwaptionGreeks_gb300.cpp")
+MKL_STANDIN = os.path.join(PKG, "shim", "include")
+
+
+def build_dropin(reference_root: str, out_dir: str, double: bool = True) -> str:
+    """Links the reference's own driver (LiborMarketModel/main.cpp, unmodified,
+    from `reference_root`) with the drop-in shim and this library: the check
+    that a user of the reference can switch by replacing two source files.
+    Returns the executable's path."""
+    lmm_dir = os.path.join(reference_root, "LiborMarketModel")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "liborSwaptionGreeks_gb300" + ("" if double else "_f32"))
+    cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++11", "-fopenmp", "-w", "-I" + lmm_dir,
+           "-I" + INCLUDE, "-I" + MKL_STANDIN, os.path.join(lmm_dir, "main.cpp"), SHIM,
+           "-L" + PKG, "-llmm_gb300", "-Wl,-rpath," + PKG, "-o", exe]
+    if double:
+        cmd.insert(1, "-DUSE_DOUBLE")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"drop-in build failed:\n{r.stdout}\n{r.stderr}")
+    return exe
+
+
 def build_cli(force: bool = False) -> str:
     """The benchmark driver (cli/lmm_bench.cpp), linked against the library
     beside it (rpath $ORIGIN)."""
