@@ -232,6 +232,8 @@ int plan(lmm_engine *e, int64_t nvs, int64_t paths, int block, int bps, int nout
     w->items = (int)items;
     w->ppt = (int)ppt;
     w->nout = nout;
+    // FP32 kernels: one wave of blocks, each looping over its units
+    w->grid = (int)std::min<int64_t>(nvs * items, std::max<int64_t>(1, (int64_t)e->sms * bps));
     LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)(nvs * items) * 2 * nout));
     w->partial = e->partial.as<double>();
     return LMM_OK;
@@ -276,7 +278,7 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     const int per_batch = fam == 1 ? block : block / 32;
     Work w{};
     LMM_TRY(plan(e, e->nscen, paths, per_batch, bps, nout, &w));
-    if (fam == 2) LMM_TRY(wpp_scratch(e, (int64_t)e->nscen * w.items, &tape));
+    if (fam == 2) LMM_TRY(wpp_scratch(e, w.grid, &tape));
     LMM_TRY(e->flag.ensure(sizeof(int)));
     LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
     mark(e, 0);
@@ -830,6 +832,7 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
         w.items = (int)citems[c];
         w.ppt = (int)cppt[c];
         w.nout = nout;
+        w.grid = (int)std::min<int64_t>(citems[c], (int64_t)e->sms * bps);
         w.partial = part;
         const float *zc = dz + (size_t)cfirst[c] * e->nmat;
         cudaError_t err = fam == 1

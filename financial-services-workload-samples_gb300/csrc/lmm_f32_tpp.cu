@@ -450,14 +450,9 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int scen = blockIdx.x / w.items, item = blockIdx.x % w.items;
     for (int i = tid; i < PAD + NN; i += B) {
         const int k = i - PAD;
         kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
-    }
-    for (int i = tid; i < NN; i += B) {
-        l0_s[i] = m.L0f[scen * NN + i];
-        il0_s[i] = m.invL0f[scen * NN + i];
     }
     for (int i = tid; i <= M; i += B) ost_s[i] = m.opt_start[i];
     for (int i = tid; i < m.nopt; i += B) {
@@ -467,96 +462,108 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         owd_s[i] = m.optWd[i];
     }
     double *acc = acc_s + warp * 2 * NOUT;
-    for (int i = tid; i < Lay::NW * 2 * NOUT; i += B) acc_s[i] = 0.0;
-    __syncthreads();
-
     const float delta = m.delta, sqd = m.sqd;
     const int64_t total = (int64_t)m.nscen * w.paths;
-    const int64_t ibase = (int64_t)item * w.ppt * B;
-    const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
     const float4 *kc0 = kc_s + PAD;
     float *vg0 = vg_s + PAD * B + tid;
     float *vt0 = vt_s + tid;
 
-    for (int j = 0; j < w.ppt; ++j) {
-        if (ibase + (int64_t)j * B >= w.paths) break;          // block-uniform
-        const int64_t pl = ibase + (int64_t)j * B + tid;
-        const bool active = pl < w.paths;
-        const int64_t pc = active ? pl : w.paths - 1;
-        const int64_t tp = (int64_t)scen * w.paths + pc;
-        const float *zp = PHILOX ? nullptr : z + pc * NMAT;
-        const uint64_t gpath = (uint64_t)(path0 + pc);
-        float *tape_v = tape ? tape + (int64_t)NN * total + tp : nullptr;
+    // Units (scenario, item) in a block-stride loop: with a grid of one wave,
+    // every block starts together and runs equal units, so the blocks of an
+    // SM stay on the same stretch of code (instruction cache).
+    const int units = m.nscen * w.items;
+    for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+        const int scen = unit / w.items, item = unit % w.items;
+        __syncthreads();          // the previous unit's reads of l0/il0/acc are done
+        for (int i = tid; i < NN; i += B) {
+            l0_s[i] = m.L0f[scen * NN + i];
+            il0_s[i] = m.invL0f[scen * NN + i];
+        }
+        for (int i = tid; i < Lay::NW * 2 * NOUT; i += B) acc_s[i] = 0.0;
+        __syncthreads();
 
-        float L[NN];
-        float Pb[NN];
-        float4 zq, zq_next;
+        const int64_t ibase = (int64_t)item * w.ppt * B;
+        const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
+        for (int j = 0; j < w.ppt; ++j) {
+            if (ibase + (int64_t)j * B >= w.paths) break;          // block-uniform
+            const int64_t pl = ibase + (int64_t)j * B + tid;
+            const bool active = pl < w.paths;
+            const int64_t pc = active ? pl : w.paths - 1;
+            const int64_t tp = (int64_t)scen * w.paths + pc;
+            const float *zp = PHILOX ? nullptr : z + pc * NMAT;
+            const uint64_t gpath = (uint64_t)(path0 + pc);
+            float *tape_v = tape ? tape + (int64_t)NN * total + tp : nullptr;
 
-        if (MODE != Mode::Backward) {
+            float L[NN];
+            float Pb[NN];
+            float4 zq, zq_next;
+
+            if (MODE != Mode::Backward) {
 #pragma unroll
-            for (int i = 0; i < NN; ++i) L[i] = l0_s[i];
-            zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
-            forward_all<NN, NMAT, PHILOX, MODE>(L, kc0, zq, zq_next, zp, seed, gpath, sqd, delta, vt0,
-                                                tape_v, total, active);
-            if (MODE == Mode::Forward && active) {
+                for (int i = 0; i < NN; ++i) L[i] = l0_s[i];
+                zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
+                forward_all<NN, NMAT, PHILOX, MODE>(L, kc0, zq, zq_next, zp, seed, gpath, sqd, delta, vt0,
+                                                    tape_v, total, active);
+                if (MODE == Mode::Forward && active) {
 #pragma unroll
-                for (int i = 0; i < NN; ++i) tape[(int64_t)i * total + tp] = L[i];
+                    for (int i = 0; i < NN; ++i) tape[(int64_t)i * total + tp] = L[i];
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < NN; ++i) L[i] = tape[(int64_t)i * total + tp];
             }
-        } else {
-#pragma unroll
-            for (int i = 0; i < NN; ++i) L[i] = tape[(int64_t)i * total + tp];
-        }
 
-        double disc = 1.0;
-        unsigned long long mask = 0ull;
-        // B[m] goes to this thread's vega column, unused until the reverse sweep.
-        float *Bst = MODE == Mode::Forward ? nullptr : vg0;
-        const double V = payoff_forward<NN, NMAT, B>(L, delta, ost_s, okd_s, owd_s, &disc, Bst, &mask);
+            double disc = 1.0;
+            unsigned long long mask = 0ull;
+            // B[m] goes to this thread's vega column, unused until the reverse sweep.
+            float *Bst = MODE == Mode::Forward ? nullptr : vg0;
+            const double V = payoff_forward<NN, NMAT, B>(L, delta, ost_s, okd_s, owd_s, &disc, Bst, &mask);
 
-        if (MODE != Mode::Forward) {
-            payoff_adjoint<NN, NMAT, B>(L, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s, owf_s);
-#pragma unroll
-            for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
-            zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);
-            reverse_all<NN, NMAT, PHILOX, MODE>(L, Pb, kc0, vg0, zq, zq_next, zp, seed, gpath, sqd, delta,
-                                                vt0, tape_v, total);
-        }
-
-        // ---- cross-path reduction of this batch of B paths ----
-        if (MODE != Mode::Backward) {
-            const float v = active ? (float)V : 0.0f;
-            const float s1 = warp_sum(v), s2 = warp_sum(v * v);
-            if (lane == 0) {
-                acc[0] += (double)s1;
-                acc[NOUT] += (double)s2;
-            }
-        }
-        if (MODE != Mode::Forward) {
-            constexpr int voff = MODE == Mode::Fused ? 1 + NN : NN;
-            constexpr int doff = MODE == Mode::Fused ? 1 : 0;
-            float *vgw = vg_s + PAD * B;
-            if (!active) {
+            if (MODE != Mode::Forward) {
+                payoff_adjoint<NN, NMAT, B>(L, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s, owf_s);
 #pragma unroll
                 for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+                zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);
+                reverse_all<NN, NMAT, PHILOX, MODE>(L, Pb, kc0, vg0, zq, zq_next, zp, seed, gpath, sqd, delta,
+                                                    vt0, tape_v, total);
             }
-            __syncwarp();
-            column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, voff);
-            __syncwarp();
-#pragma unroll
-            for (int i = 0; i < NN; ++i) vg0[i * B] = active ? Pb[i] * il0_s[i] : 0.0f;
-            __syncwarp();
-            column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, doff);
-            __syncwarp();
-        }
-    }
 
-    __syncthreads();
-    for (int o = tid; o < 2 * NOUT; o += B) {
-        double s = 0.0;
+            // ---- cross-path reduction of this batch of B paths ----
+            if (MODE != Mode::Backward) {
+                const float v = active ? (float)V : 0.0f;
+                const float s1 = warp_sum(v), s2 = warp_sum(v * v);
+                if (lane == 0) {
+                    acc[0] += (double)s1;
+                    acc[NOUT] += (double)s2;
+                }
+            }
+            if (MODE != Mode::Forward) {
+                constexpr int voff = MODE == Mode::Fused ? 1 + NN : NN;
+                constexpr int doff = MODE == Mode::Fused ? 1 : 0;
+                float *vgw = vg_s + PAD * B;
+                if (!active) {
 #pragma unroll
-        for (int q = 0; q < Lay::NW; ++q) s += acc_s[q * 2 * NOUT + o];
-        w.partial[(size_t)blockIdx.x * 2 * NOUT + o] = s;
-    }
+                    for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+                }
+                __syncwarp();
+                column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, voff);
+                __syncwarp();
+#pragma unroll
+                for (int i = 0; i < NN; ++i) vg0[i * B] = active ? Pb[i] * il0_s[i] : 0.0f;
+                __syncwarp();
+                column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, doff);
+                __syncwarp();
+            }
+        }
+
+        __syncthreads();
+        for (int o = tid; o < 2 * NOUT; o += B) {
+            double s = 0.0;
+#pragma unroll
+            for (int q = 0; q < Lay::NW; ++q) s += acc_s[q * 2 * NOUT + o];
+            w.partial[(size_t)unit * 2 * NOUT + o] = s;
+        }
+    }  // units
 }
 
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
@@ -567,7 +574,7 @@ cudaError_t launch_tpp(const DevModel &m, const float *z, uint64_t seed, int64_t
     auto kern = k_tpp<NN, NMAT, PHILOX, MODE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
     if (e != cudaSuccess) return e;
-    const unsigned grid = (unsigned)((int64_t)m.nscen * w.items);
+    const unsigned grid = (unsigned)(w.grid > 0 ? w.grid : (int64_t)m.nscen * w.items);
     kern<<<grid, kTppBlock, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar);
     return cudaGetLastError();
 }

@@ -219,8 +219,8 @@ struct ZChunk {
 // MODE: Fused (value + all Greeks), Forward (value only) or Backward (Greeks
 // of vbar[scen] x value; the forward is recomputed from the same normals, so
 // no tape is needed). ytop: gridDim.x * kWppWarps blocks of
-// wpp_scratch_floats(nmat, S) floats of scratch, one per warp (unused in
-// Forward mode).
+// wpp_scratch_floats(nmat, S) floats of scratch, one per resident warp
+// (unused in Forward mode).
 template <int S, bool PHILOX, Mode MODE>
 __global__ void __launch_bounds__(kWppBlock, wpp_min_blocks(S))
 k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
@@ -247,12 +247,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     float *bw_s = reinterpret_cast<float *>(wbase + Ly.bw);
     double *acc = reinterpret_cast<double *>(wbase + Ly.acc);
 
-    const int scen = blockIdx.x / w.items, item = blockIdx.x % w.items;
     for (int i = tid; i <= nn; i += kWppBlock) kc_s[i] = i == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[i - 1];
-    for (int i = tid; i < nn; i += kWppBlock) {
-        l0_s[i] = m.L0f[scen * nn + i];
-        il0_s[i] = m.invL0f[scen * nn + i];
-    }
     for (int i = tid; i <= M; i += kWppBlock) ost_s[i] = m.opt_start[i];
     for (int i = tid; i < m.nopt; i += kWppBlock) {
         okf_s[i] = m.optKf[i];
@@ -260,9 +255,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         owf_s[i] = m.optWf[i];
         owd_s[i] = m.optWd[i];
     }
-    for (int i = lane; i < 2 * nout; i += 32) acc[i] = 0.0;
     for (int i = lane; i <= 32 * S; i += 32) vg_s[i] = 0.0f;
-    __syncthreads();
 
     int base[S];
 #pragma unroll
@@ -270,142 +263,156 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         const int i = S * lane + s;
         base[s] = i < nn ? i : 0;
     }
-
     const float delta = m.delta, sqd = m.sqd, d2 = m.d2;
-    const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
-    const int64_t ibase = (int64_t)item * w.ppt * kWppWarps;
-    for (int j = 0; j < w.ppt; ++j) {
-        const int64_t p = ibase + (int64_t)j * kWppWarps + warp;
-        if (p >= w.paths) break;                                  // warp-uniform
-        const float *zp = PHILOX ? nullptr : z + p * nmat;
-        const uint64_t gpath = (uint64_t)(path0 + p);
-        ZChunk<PHILOX> zc;
 
-        float L[S], Pb[S];
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const int i = S * lane + s;
-            L[s] = i < nn ? l0_s[i] : 1.0f;
+    // Units (scenario, item) in a block-stride loop over a grid of one wave
+    // (blocks start together and stay on the same code).
+    const int units = m.nscen * w.items;
+    for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+        const int scen = unit / w.items, item = unit % w.items;
+        __syncthreads();          // the previous unit's reads of l0/il0 are done
+        for (int i = tid; i < nn; i += kWppBlock) {
+            l0_s[i] = m.L0f[scen * nn + i];
+            il0_s[i] = m.invL0f[scen * nn + i];
         }
-        // ---- forward ----
-        for (int n = 0; n < nmat; ++n) {
-            if (MODE != Mode::Forward && n % kWppReset == 0) {
+        for (int i = lane; i < 2 * nout; i += 32) acc[i] = 0.0;
+        __syncthreads();
+
+        const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
+        const int64_t ibase = (int64_t)item * w.ppt * kWppWarps;
+        for (int j = 0; j < w.ppt; ++j) {
+            const int64_t p = ibase + (int64_t)j * kWppWarps + warp;
+            if (p >= w.paths) break;                                  // warp-uniform
+            const float *zp = PHILOX ? nullptr : z + p * nmat;
+            const uint64_t gpath = (uint64_t)(path0 + p);
+            ZChunk<PHILOX> zc;
+
+            float L[S], Pb[S];
 #pragma unroll
-                for (int s = 0; s < S; ++s) ck[((n / kWppReset) * S + s) * 32] = L[s];
+            for (int s = 0; s < S; ++s) {
+                const int i = S * lane + s;
+                L[s] = i < nn ? l0_s[i] : 1.0f;
             }
-            const float sqez = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
-            const float y = wpp_fwd_step<S>(L, base, n, sqez, lane, kc_s, delta);
-            if (MODE != Mode::Forward) yt[n * 32] = y;
-        }
-        // ---- payoff (FP64 products) and its adjoint ----
-        double dprod = 1.0;
+            // ---- forward ----
+            for (int n = 0; n < nmat; ++n) {
+                if (MODE != Mode::Forward && n % kWppReset == 0) {
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const int i = S * lane + s;
-            if (i < nmat) dprod *= (double)__frcp_rn(fmaf(delta, L[s], 1.0f));
-            if (i < nn) lw_s[i] = L[s];
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) dprod *= __shfl_xor_sync(0xffffffffu, dprod, o);
-        const double disc = dprod;
-        __syncwarp();
-        double V = 0.0;
-        if (lane == 0) {
-            double bb = 1.0, ss = 0.0, vs = 0.0;
-            unsigned long long mask = 0ull;
-            for (int mm = 0; mm < M; ++mm) {
-                bb *= (double)__frcp_rn(fmaf(delta, lw_s[nmat + mm], 1.0f));
-                ss = fma((double)delta, bb, ss);
-                bw_s[mm] = (float)bb;
-                for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
-                    const double sw = fma(okd_s[o], ss, bb) - 1.0;
-                    if (sw < 0.0) {
-                        vs -= (100.0 * sw) * owd_s[o];
-                        mask |= 1ull << o;
-                    }
+                    for (int s = 0; s < S; ++s) ck[((n / kWppReset) * S + s) * 32] = L[s];
                 }
+                const float sqez = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
+                const float y = wpp_fwd_step<S>(L, base, n, sqez, lane, kc_s, delta);
+                if (MODE != Mode::Forward) yt[n * 32] = y;
             }
-            V = disc * vs;
-            if (MODE == Mode::Forward) mask = 0ull;     // no adjoint
-            // :173-184 with the rate kept apart from its adjoint; lw_s[i] becomes
-            // the log-adjoint of rate i >= nmat. B[m] comes from the forward
-            // (bw_s): rebuilding it backwards from the last, smallest factor
-            // would underflow FP32 on paths whose rates grow large.
-            const float scale = -vb * (float)disc * delta;
-            float Sb = 0.0f, Bb = 0.0f;
-            for (int mm = M - 1; mm >= 0; --mm) {
-                const float Ln = lw_s[nmat + mm];
-                const float r = __frcp_rn(fmaf(delta, Ln, 1.0f));
-                const float Bm = bw_s[mm];
-                for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
-                    if ((mask >> o) & 1ull) {
-                        Sb -= (100.0f * okf_s[o]) * owf_s[o];
-                        Bb -= 100.0f * owf_s[o];
-                    }
-                }
-                Bb = fmaf(delta, Sb, Bb);
-                lw_s[nmat + mm] = scale * Bb * Bm * (Ln * r);
-                Bb *= r;
+            // ---- payoff (FP64 products) and its adjoint ----
+            double dprod = 1.0;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const int i = S * lane + s;
+                if (i < nmat) dprod *= (double)__frcp_rn(fmaf(delta, L[s], 1.0f));
+                if (i < nn) lw_s[i] = L[s];
             }
-        }
-        V = __shfl_sync(0xffffffffu, V, 0);
-        __syncwarp();
-        if (MODE == Mode::Forward) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) dprod *= __shfl_xor_sync(0xffffffffu, dprod, o);
+            const double disc = dprod;
+            __syncwarp();
+            double V = 0.0;
             if (lane == 0) {
+                double bb = 1.0, ss = 0.0, vs = 0.0;
+                unsigned long long mask = 0ull;
+                for (int mm = 0; mm < M; ++mm) {
+                    bb *= (double)__frcp_rn(fmaf(delta, lw_s[nmat + mm], 1.0f));
+                    ss = fma((double)delta, bb, ss);
+                    bw_s[mm] = (float)bb;
+                    for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
+                        const double sw = fma(okd_s[o], ss, bb) - 1.0;
+                        if (sw < 0.0) {
+                            vs -= (100.0 * sw) * owd_s[o];
+                            mask |= 1ull << o;
+                        }
+                    }
+                }
+                V = disc * vs;
+                if (MODE == Mode::Forward) mask = 0ull;     // no adjoint
+                // :173-184 with the rate kept apart from its adjoint; lw_s[i] becomes
+                // the log-adjoint of rate i >= nmat. B[m] comes from the forward
+                // (bw_s): rebuilding it backwards from the last, smallest factor
+                // would underflow FP32 on paths whose rates grow large.
+                const float scale = -vb * (float)disc * delta;
+                float Sb = 0.0f, Bb = 0.0f;
+                for (int mm = M - 1; mm >= 0; --mm) {
+                    const float Ln = lw_s[nmat + mm];
+                    const float r = __frcp_rn(fmaf(delta, Ln, 1.0f));
+                    const float Bm = bw_s[mm];
+                    for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
+                        if ((mask >> o) & 1ull) {
+                            Sb -= (100.0f * okf_s[o]) * owf_s[o];
+                            Bb -= 100.0f * owf_s[o];
+                        }
+                    }
+                    Bb = fmaf(delta, Sb, Bb);
+                    lw_s[nmat + mm] = scale * Bb * Bm * (Ln * r);
+                    Bb *= r;
+                }
+            }
+            V = __shfl_sync(0xffffffffu, V, 0);
+            __syncwarp();
+            if (MODE == Mode::Forward) {
+                if (lane == 0) {
+                    acc[0] += V;
+                    acc[nout] += V * V;
+                }
+                continue;
+            }
+            const float vsd = -vb * (float)V * delta;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const int i = S * lane + s;
+                if (i < nmat) Pb[s] = vsd * (L[s] * __frcp_rn(fmaf(delta, L[s], 1.0f)));
+                else Pb[s] = i < nn ? lw_s[i] : 0.0f;
+            }
+            // ---- reverse: each step rebuilt from the forward's Y_top ----
+            float ynext = yt[(nmat - 1) * 32];
+            for (int n = nmat - 1; n >= 0; --n) {
+                const float y = ynext;
+                if (n > 0) ynext = yt[(n - 1) * 32];
+                wpp_rev_step<S>(L, Pb, base, n, lane, y, kc_s, vg_s, delta, d2);
+                if (n % kWppReset == 0) {
+#pragma unroll
+                    for (int s = 0; s < S; ++s) L[s] = ck[((n / kWppReset) * S + s) * 32];
+                }
+            }
+            // ---- accumulate this path: value, deltas, vegas ----
+            __syncwarp();
+            constexpr int doff = MODE == Mode::Fused ? 1 : 0;   // deltas at doff, vegas at doff + nn
+            if (MODE == Mode::Fused && lane == 0) {
                 acc[0] += V;
                 acc[nout] += V * V;
             }
-            continue;
-        }
-        const float vsd = -vb * (float)V * delta;
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const int i = S * lane + s;
-            if (i < nmat) Pb[s] = vsd * (L[s] * __frcp_rn(fmaf(delta, L[s], 1.0f)));
-            else Pb[s] = i < nn ? lw_s[i] : 0.0f;
-        }
-        // ---- reverse: each step rebuilt from the forward's Y_top ----
-        float ynext = yt[(nmat - 1) * 32];
-        for (int n = nmat - 1; n >= 0; --n) {
-            const float y = ynext;
-            if (n > 0) ynext = yt[(n - 1) * 32];
-            wpp_rev_step<S>(L, Pb, base, n, lane, y, kc_s, vg_s, delta, d2);
-            if (n % kWppReset == 0) {
-#pragma unroll
-                for (int s = 0; s < S; ++s) L[s] = ck[((n / kWppReset) * S + s) * 32];
+            for (int s = 0; s < S; ++s) {
+                const int i = S * lane + s;
+                if (i < nn) {
+                    const double dl = (double)(Pb[s] * il0_s[i]);
+                    acc[doff + i] += dl;
+                    acc[nout + doff + i] += dl * dl;
+                }
             }
-        }
-        // ---- accumulate this path: value, deltas, vegas ----
-        __syncwarp();
-        constexpr int doff = MODE == Mode::Fused ? 1 : 0;   // deltas at doff, vegas at doff + nn
-        if (MODE == Mode::Fused && lane == 0) {
-            acc[0] += V;
-            acc[nout] += V * V;
-        }
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const int i = S * lane + s;
-            if (i < nn) {
-                const double dl = (double)(Pb[s] * il0_s[i]);
-                acc[doff + i] += dl;
-                acc[nout + doff + i] += dl * dl;
+            for (int k = lane; k < nn; k += 32) {
+                const double vgk = (double)vg_s[k + 1];
+                acc[doff + nn + k] += vgk;
+                acc[nout + doff + nn + k] += vgk * vgk;
+                vg_s[k + 1] = 0.0f;
             }
+            __syncwarp();
         }
-        for (int k = lane; k < nn; k += 32) {
-            const double vgk = (double)vg_s[k + 1];
-            acc[doff + nn + k] += vgk;
-            acc[nout + doff + nn + k] += vgk * vgk;
-            vg_s[k + 1] = 0.0f;
+        __syncthreads();
+        for (int o = tid; o < 2 * nout; o += kWppBlock) {
+            double s = 0.0;
+            for (int q = 0; q < kWppWarps; ++q)
+                s += reinterpret_cast<const double *>(smem + Ly.warp0 + q * Ly.per_warp + Ly.acc)[o];
+            w.partial[(size_t)unit * 2 * nout + o] = s;
         }
-        __syncwarp();
-    }
-    __syncthreads();
-    for (int o = tid; o < 2 * nout; o += kWppBlock) {
-        double s = 0.0;
-        for (int q = 0; q < kWppWarps; ++q)
-            s += reinterpret_cast<const double *>(smem + Ly.warp0 + q * Ly.per_warp + Ly.acc)[o];
-        w.partial[(size_t)blockIdx.x * 2 * nout + o] = s;
-    }
+    }  // units
 }
 
 template <int S, bool PHILOX, Mode MODE>
@@ -416,7 +423,8 @@ cudaError_t wpp_launch_s(const DevModel &m, const float *z, uint64_t seed, int64
     auto kern = k_wpp<S, PHILOX, MODE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    kern<<<(unsigned)((int64_t)m.nscen * w.items), kWppBlock, bytes, st>>>(m, z, seed, path0, w, vbar, ytop);
+    const unsigned grid = (unsigned)(w.grid > 0 ? w.grid : (int64_t)m.nscen * w.items);
+    kern<<<grid, kWppBlock, bytes, st>>>(m, z, seed, path0, w, vbar, ytop);
     return cudaGetLastError();
 }
 

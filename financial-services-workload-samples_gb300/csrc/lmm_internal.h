@@ -40,6 +40,8 @@ struct Work {
     int ppt;              // paths per thread per item
     double *partial;      // [nscen*items][2*nout]: per-item sums and sums of squares
     int nout;             // outputs per scenario reduced by this launch
+    int grid = 0;         // FP32 kernels: blocks launched (0: one per unit); block b
+                          // runs units b, b+grid, ... of the nscen*items units
 };
 
 enum class Mode : int { Fused = 0, Forward = 1, Backward = 2 };
