@@ -44,11 +44,13 @@
 // fixed order, so results are bit-reproducible.
 #include "lmm_device.cuh"
 
+// 128 threads (4 warps) per block, 2 blocks per SM: 248 registers per thread
+// leave room for 8 warps per SM.
 #ifndef LMM_TPP_BLOCK
-#define LMM_TPP_BLOCK 64
+#define LMM_TPP_BLOCK 128
 #endif
 #ifndef LMM_TPP_MINB
-#define LMM_TPP_MINB 4
+#define LMM_TPP_MINB 2
 #endif
 // Reverse steps processed together as a skewed wavefront (independent
 // reconstruction chains per instruction stream): 2 or 4.
@@ -63,6 +65,14 @@
 // cell in each phase (4.6% faster on GB300), at the price of accumulating the
 // drift on top of the normal term (FP32 vs FP64 Greek errors about 15% larger,
 // still 1e-6 of the 1e-4 bound).
+// 1: a block barrier per forward step pair and reverse step group, so that
+// the warps of a block stay on the same stretch of the unrolled bodies
+// (instruction cache). Without it, blocks that run long drift apart: on 256
+// curve scenarios x 262,144 paths (GB300) 310 ms without, 243 ms with; equal
+// on one scenario.
+#ifndef LMM_TPP_SYNC
+#define LMM_TPP_SYNC 1
+#endif
 #ifndef LMM_TPP_YRUN
 #define LMM_TPP_YRUN 1
 #endif
@@ -375,6 +385,7 @@ __device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, f
     if constexpr (MODE == Mode::Fused) {
         static_assert(NMAT % 2 == 0, "paired forward steps");
         for (int n = 0; n < NMAT; n += 2) {
+            if (LMM_TPP_SYNC) __syncthreads();
             if ((n & 3) == 0) {
                 zq = zq_next;
                 if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
@@ -410,6 +421,7 @@ __device__ __forceinline__ void reverse_all(float (&L)[NN], float (&Pb)[NN], con
     static_assert(NMAT % G == 0 && (G == 2 || G == 4), "whole step groups");
     constexpr int B = kTppBlock;
     for (int n = NMAT - 1; n > 0; n -= G) {
+        if (LMM_TPP_SYNC) __syncthreads();
         if ((n & 3) == 3) {
             zq = zq_next;
             if ((n >> 2) > 0) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) - 1);
