@@ -135,7 +135,7 @@ k_f64_greeks(const DevModel m, const double *__restrict__ z, const Work w)
                 const double l = lam_s[i - n - 1];
                 const double con1 = d * l;
                 const double wexp = con1 * v + l * (sqez - 0.5 * con1);
-                const double Ln = L[i] / exp(wexp);          // L_{n,i} from L_{n+1,i}
+                const double Ln = L[i] * exp(-wexp);         // L_{n,i} from L_{n+1,i}
                 const double r = 1.0 / (1.0 + d * Ln);
                 const double t = Ln * r;
                 const double pb = Pb[i];
