@@ -94,7 +94,12 @@ const char *lmm_version(void);
 /* Uploads the parameters to `device` and creates the engine's own stream. */
 int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out);
 int lmm_engine_destroy(lmm_engine *e);
-/* Use `stream` (a cudaStream_t, NULL = legacy default stream) from now on. */
+/* Use `stream` (a cudaStream_t, NULL = legacy default stream) from now on.
+ * CUDA graphs: once a device call (lmm_greeks_f32_device, lmm_greeks_philox_device,
+ * lmm_greeks_f64_device, the mrg32k3a/normals generators) has run for a
+ * given engine and path count, repeating it enqueues only kernels and async
+ * memsets on the stream and allocates nothing, so it can be recorded by a
+ * stream capture and replayed. */
 int lmm_engine_set_stream(lmm_engine *e, void *stream);
 /* Blocks until all work enqueued on the engine's stream is done. */
 int lmm_engine_synchronize(lmm_engine *e);
