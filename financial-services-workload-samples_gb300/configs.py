@@ -7,7 +7,8 @@ own set bit for bit, and ``workload`` builds the five named workloads:
 
   1. NN=80/NMAT=40, flat L0=0.05, flat lambda=0.2, 15 swaptions, 65,536 paths (FP64)
   2. same model, 4,194,304 paths, FP32 normals read from HBM (the headline)
-  3. NN=160/NMAT=120, random L0/lambda, 30 swaptions, 1,048,576 paths, checkpoints every 8 steps
+  3. NN=160/NMAT=120, random L0/lambda, 30 swaptions, 1,048,576 paths, rates saved
+     every 8 steps for the reverse sweep
   4. NN=80/NMAT=40, lambda[i]=0.15+0.1exp(-0.05i), L0[i]=0.03+0.0005i, 16,777,216 paths, in-kernel Philox
   5. 256 curves x 262,144 paths in one launch
 """
@@ -47,7 +48,8 @@ class LmmConfig:
     paths: int
     normals: str = "hbm"          # "hbm": pre-generated array; "philox": in-kernel
     seed: int = 1
-    ckpt_every: int = 0           # 0: not applicable to the kernel chosen
+    ckpt_every: int = 0           # steps between the rate snapshots the reverse sweep
+                                  # restores (warp-per-path kernel); 0: none
     extra: dict = field(default_factory=dict)
 
     @property
