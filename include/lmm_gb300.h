@@ -34,7 +34,10 @@
  *   - *_host calls take host pointers and block until results are back.
  *     *_device calls take device pointers, are enqueued on the engine's
  *     stream and return without waiting.
- *   - One engine is not thread-safe; distinct engines are independent.
+ *   - One engine is not thread-safe; distinct engines are independent and may
+ *     be driven from different host threads at once. The reference-signature
+ *     calls share one internal engine behind a lock and may be called from
+ *     any thread.
  */
 #ifndef LMM_GB300_H
 #define LMM_GB300_H
