@@ -18,8 +18,8 @@
 // replaces the rebuilt rates by the saved ones, so FP32 rounding of the
 // reconstruction accumulates over at most kWppReset steps. The adjoint in log form
 // (Pb = L dV/dL) is
-//   S_i = sum_{j>=i} lambda_k Pb_j,  Pb_i += delta^2 lambda_k t r S_i
-//   dV/dlambda_k += Pb_i (Y_i - delta lambda_k) + delta^2 t S_i.
+//   S'_i = delta^2 sum_{j>=i} lambda_k Pb_j,  Pb_i += lambda_k t r S'_i
+//   dV/dlambda_k += Pb_i (Y_i - delta lambda_k) + t S'_i.
 // The payoff (portfolio_b :120-211, aliasing fixed) runs with FP64 products:
 // the discount product is a warp product reduction, the annuity recursion
 // runs on lane 0.
@@ -149,11 +149,12 @@ __device__ __forceinline__ float wpp_fwd_step(float (&L)[S], const int (&base)[S
 
 // Reverse step n (path_calc_b2 :100-112 in log-adjoint form) + vega: L holds
 // L_{n+1} on entry and L_n on exit; ytop is the forward's Y at the lane's top
-// slot. The suffix sum takes the log-adjoints before the step's update.
+// slot. The suffix sum, taken over the log-adjoints before the step's update,
+// is carried as S' = delta^2 S (sums of delta^2 lambda_k Pb), so that
+// Pb += lambda_k r t S' and the vega term t S' need no further factor.
 template <int S>
 __device__ __forceinline__ void wpp_rev_step(float (&L)[S], float (&Pb)[S], const int (&base)[S], int n,
-                                             int lane, float ytop, const float4 *kc, float *vg, float delta,
-                                             float d2)
+                                             int lane, float ytop, const float4 *kc, float *vg, float delta)
 {
     float b[S];
     float4 kk[S];
@@ -161,7 +162,7 @@ __device__ __forceinline__ void wpp_rev_step(float (&L)[S], float (&Pb)[S], cons
 #pragma unroll
     for (int s = S - 1; s >= 0; --s) {
         kk[s] = kc[wpp_row(base, s, n)];
-        Q = fmaf(kk[s].w, Pb[s], Q);
+        Q = fmaf(kk[s].z, Pb[s], Q);
         b[s] = Q;                                   // local inclusive suffix
     }
     const float Yx = warp_excl_suffix(Q, lane);
@@ -172,8 +173,8 @@ __device__ __forceinline__ void wpp_rev_step(float (&L)[S], float (&Pb)[S], cons
         const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
         const float t = Ln * r;
         const float tS = t * (Yx + b[s]);
-        vg[wpp_row(base, s, n)] += fmaf(Pb[s], fmaf(-delta, kk[s].w, Y), d2 * tS);
-        Pb[s] = fmaf(kk[s].z * r, tS, Pb[s]);
+        vg[wpp_row(base, s, n)] += fmaf(Pb[s], fmaf(-delta, kk[s].w, Y), tS);
+        Pb[s] = fmaf(kk[s].w * r, tS, Pb[s]);
         L[s] = Ln;
         Y = fmaf(-kk[s].z, t, Y);
     }
@@ -263,7 +264,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         const int i = S * lane + s;
         base[s] = i < nn ? i : 0;
     }
-    const float delta = m.delta, sqd = m.sqd, d2 = m.d2;
+    const float delta = m.delta, sqd = m.sqd;
 
     // Units (scenario, item) in a block-stride loop over a grid of one wave
     // (blocks start together and stay on the same code).
@@ -375,7 +376,7 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             for (int n = nmat - 1; n >= 0; --n) {
                 const float y = ynext;
                 if (n > 0) ynext = yt[(n - 1) * 32];
-                wpp_rev_step<S>(L, Pb, base, n, lane, y, kc_s, vg_s, delta, d2);
+                wpp_rev_step<S>(L, Pb, base, n, lane, y, kc_s, vg_s, delta);
                 if (n % kWppReset == 0) {
 #pragma unroll
                     for (int s = 0; s < S; ++s) L[s] = ck[((n / kWppReset) * S + s) * 32];
