@@ -30,6 +30,13 @@ namespace {
 
 constexpr int kWppBlock = 128;
 constexpr int kWppWarps = kWppBlock / 32;
+// 1: the constant and vega tables carry nmat zero/discard rows in front, so a
+// cell's row is base - n without a clamp (3.8 KB more shared memory per
+// block at 160/120, still 6 blocks per SM; 1.4% faster on GB300). 0: one
+// head row and row max(base - n, 0).
+#ifndef LMM_WPP_PAD
+#define LMM_WPP_PAD 1
+#endif
 #ifndef LMM_WPP_RESET
 #define LMM_WPP_RESET 8
 #endif
@@ -58,6 +65,10 @@ struct WppLay {
     size_t kc, l0, il0, ost, okf, okd, owf, owd, warp0, per_warp, vg, lw, bw, acc, bytes;
 };
 
+// Rows in front of the tables: row k + head holds k; rows below head are zero
+// (constants) or discarded (vegas).
+__host__ __device__ constexpr int wpp_head(int nmat) { return LMM_WPP_PAD ? nmat : 1; }
+
 __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S, Mode mode = Mode::Fused)
 {
     WppLay L{};
@@ -67,7 +78,7 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S, Mode mode 
     L.M = nn - nmat;
     L.nout = mode == Mode::Fused ? 1 + 2 * nn : (mode == Mode::Forward ? 1 : 2 * nn);
     size_t o = 0;
-    L.kc = o; o = al16(o + 16 * (size_t)(nn + 1));    // [0]: zeros, [k+1]: constants of k
+    L.kc = o; o = al16(o + 16 * (size_t)(nn + wpp_head(nmat)));   // head zero rows, then constants of k
     L.l0 = o; o = al16(o + 4 * (size_t)nn);
     L.il0 = o; o = al16(o + 4 * (size_t)nn);
     L.ost = o; o = al16(o + 4 * (size_t)(L.M + 1));
@@ -77,7 +88,7 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S, Mode mode 
     L.owd = o; o = al16(o + 8 * (size_t)kMaxNopt);
     L.warp0 = o;
     size_t w = 0;
-    L.vg = w; w = al16(w + 4 * (size_t)(32 * S + 1));     // vegas [1+32*S] (row k+1; row 0 discards)
+    L.vg = w; w = al16(w + 4 * (size_t)(32 * S + wpp_head(nmat)));   // head rows discard, then vegas
     L.lw = w; w = al16(w + 4 * (size_t)32 * S);           // payoff staging [32*S]
     L.bw = w; w = al16(w + 4 * (size_t)32 * S);           // annuity factors B[m] [32*S]
     L.acc = w; w = al16(w + 8 * (size_t)2 * L.nout);      // FP64 sums [2*nout]
@@ -113,16 +124,18 @@ __device__ __forceinline__ float warp_excl_suffix(float x, int lane)
     return lane == 31 ? 0.0f : ex;
 }
 
-// Constants and vega row of slot s at step n: row max(base[s] - n, 0) of the
-// tables, whose row 0 is zero (constants) or discarded (vegas) and row k+1
-// holds k. base[s] = i for a real rate i < nn (row i-n = k+1 for k = i-n-1
-// >= 0, row 0 for a rate not yet moving), 0 for a padding slot (i >= nn). A
+// Constants and vega row of slot s at step n. The tables hold k at row
+// k + head; the rows below head are zero (constants) or discarded (vegas).
+// base[s] = i + head - 1 for a real rate i < nn, so row base - n belongs to
+// k = i-n-1 (a rate not yet moving, k < 0, lands below head), and head - 1
+// for a padding slot (i >= nn), which stays below head for every step. With
+// head = nmat no clamp is needed; with head = 1 the row is clamped at 0. A
 // zero row makes the cell an exact no-op: L *= 2^0, the sums gain 0 and Pb
 // keeps its value, so the steps need no per-slot branches.
 template <int S>
 __device__ __forceinline__ int wpp_row(const int (&base)[S], int s, int n)
 {
-    return max(base[s] - n, 0);
+    return LMM_WPP_PAD ? base[s] - n : max(base[s] - n, 0);
 }
 
 // One forward step n over the lane's slots; returns Y at the lane's top slot
@@ -248,7 +261,9 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     float *bw_s = reinterpret_cast<float *>(wbase + Ly.bw);
     double *acc = reinterpret_cast<double *>(wbase + Ly.acc);
 
-    for (int i = tid; i <= nn; i += kWppBlock) kc_s[i] = i == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[i - 1];
+    const int head = wpp_head(nmat);
+    for (int i = tid; i < nn + head; i += kWppBlock)
+        kc_s[i] = i < head ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[i - head];
     for (int i = tid; i <= M; i += kWppBlock) ost_s[i] = m.opt_start[i];
     for (int i = tid; i < m.nopt; i += kWppBlock) {
         okf_s[i] = m.optKf[i];
@@ -256,13 +271,13 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         owf_s[i] = m.optWf[i];
         owd_s[i] = m.optWd[i];
     }
-    for (int i = lane; i <= 32 * S; i += 32) vg_s[i] = 0.0f;
+    for (int i = lane; i < 32 * S + head; i += 32) vg_s[i] = 0.0f;
 
     int base[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) {
         const int i = S * lane + s;
-        base[s] = i < nn ? i : 0;
+        base[s] = i < nn ? i + head - 1 : head - 1;   // row of k = i-n-1 is base - n
     }
     const float delta = m.delta, sqd = m.sqd;
 
@@ -399,10 +414,10 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 }
             }
             for (int k = lane; k < nn; k += 32) {
-                const double vgk = (double)vg_s[k + 1];
+                const double vgk = (double)vg_s[k + head];
                 acc[doff + nn + k] += vgk;
                 acc[nout + doff + nn + k] += vgk * vgk;
-                vg_s[k + 1] = 0.0f;
+                vg_s[k + head] = 0.0f;
             }
             __syncwarp();
         }
