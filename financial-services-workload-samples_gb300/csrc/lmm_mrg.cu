@@ -8,7 +8,9 @@
 //   z = (x - y) mod m1 in [1, m1], u = z / (m1+1));
 //   skip-ahead by powers of the 3x3 companion matrices;
 //   M. J. Wichura, Applied Statistics 37(3), 1988, AS241: PPND16 (FP64
-//   output) and PPND7 in FP32 arithmetic (FP32 output).
+//   output) and PPND7 in FP32 arithmetic (FP32 output; its arguments
+//   q = u - 1/2 and min(u, 1-u) are formed from the integer z, so the FP32
+//   path has no FP64 operation).
 // Seeding from one 32-bit seed s: x state (s mod m1, 1, 1), y state (1,1,1).
 //
 // Work layout. Each warp owns a chunk of 32*kSpan consecutive stream
@@ -32,6 +34,8 @@ namespace {
 constexpr uint64_t kM1 = 4294967087ULL;
 constexpr uint64_t kM2 = 4294944443ULL;
 constexpr int kSpan = 512;        // elements per lane per chunk (multiple of 32)
+constexpr int64_t kHalfM1p1 = 2147483544;            // (m1 + 1) / 2
+constexpr float kNormF = (float)(1.0 / 4294967088.0); // 1 / (m1 + 1), rounded to FP32
 constexpr int kWarps = 4;         // warps per block
 
 __device__ __forceinline__ void jump(const uint32_t *m, uint64_t v[3], uint64_t mod)
@@ -114,8 +118,7 @@ __device__ double ppnd16(double p)
 
 __device__ __forceinline__ float mad_rn(float r, float x, float c) { return __fadd_rn(__fmul_rn(r, x), c); }
 
-// AS241 PPND7 in FP32 from q = p - 1/2 and pt = min(p, 1-p), both formed in
-// FP64 from the stream value.
+// AS241 PPND7 in FP32 from q = p - 1/2 and pt = min(p, 1-p).
 __device__ float ppnd7(float q, float pt)
 {
     if (fabsf(q) <= 0.425f) {
@@ -165,14 +168,18 @@ k_mrg32k3a(const MrgTables J, uint32_t seed, int64_t first, int64_t count, doubl
 #pragma unroll 4
         for (int i = 0; i < 32; ++i) {
             const uint32_t z = mrg_step(x, y);
-            const double u = (double)z * (1.0 / 4294967088.0);
-            if constexpr (KIND == 0) {
-                tile[w][lane][i] = (T)u;
-            } else if constexpr (KIND == 1) {
-                tile[w][lane][i] = (T)__dadd_rn(mean, __dmul_rn(sd, ppnd16(u)));
+            if constexpr (KIND == 2) {
+                // q = u - 1/2 and min(u, 1-u) from the integer z, in FP32 (no FP64)
+                const float q = __fmul_rn(__int2float_rn((int32_t)((int64_t)z - kHalfM1p1)), kNormF);
+                const uint32_t zt = min(z, (uint32_t)(2 * kHalfM1p1) - z);
+                const float pt = __fmul_rn(__uint2float_rn(zt), kNormF);
+                tile[w][lane][i] = __fadd_rn(fmean, __fmul_rn(fsd, ppnd7(q, pt)));
             } else {
-                const double pt = u < 0.5 ? u : 1.0 - u;
-                tile[w][lane][i] = (T)__fadd_rn(fmean, __fmul_rn(fsd, ppnd7((float)(u - 0.5), (float)pt)));
+                const double u = (double)z * (1.0 / 4294967088.0);
+                if constexpr (KIND == 0)
+                    tile[w][lane][i] = (T)u;
+                else
+                    tile[w][lane][i] = (T)__dadd_rn(mean, __dmul_rn(sd, ppnd16(u)));
             }
         }
         __syncwarp();

@@ -106,7 +106,8 @@ static void seed_state(uint32_t seed, uint64_t x[3], uint64_t y[3])
     y[0] = y[1] = y[2] = 1;
 }
 
-static double next_u(uint64_t x[3], uint64_t y[3])
+/* One step of both recurrences; returns z in [1, m1]. */
+static uint32_t next_z(uint64_t x[3], uint64_t y[3])
 {
     /* each product is below 2^53, so the differences fit in int64 */
     int64_t p1 = ((int64_t)(1403580ULL * x[1]) - (int64_t)(810728ULL * x[0])) % (int64_t)M1;
@@ -119,9 +120,10 @@ static double next_u(uint64_t x[3], uint64_t y[3])
     y[0] = y[1];
     y[1] = y[2];
     y[2] = (uint64_t)p2;
-    const int64_t z = p1 > p2 ? p1 - p2 : p1 - p2 + (int64_t)M1;
-    return (double)z * (1.0 / 4294967088.0);
+    return (uint32_t)(p1 > p2 ? p1 - p2 : p1 - p2 + (int64_t)M1);
 }
+
+static double next_u(uint64_t x[3], uint64_t y[3]) { return (double)next_z(x, y) * (1.0 / 4294967088.0); }
 
 /* Sequential stream elements [first, first+count) as uniforms in (0,1). */
 void lmmo_mrg32k3a_uniforms(uint32_t seed, int64_t first, int64_t count, double *u)
@@ -187,8 +189,8 @@ double lmmo_ppnd16(double p)
 }
 
 /* AS241 PPND7 in FP32 arithmetic. The caller passes q = p - 1/2 and the
- * smaller tail probability pt = min(p, 1-p), both formed in FP64 from the
- * integer stream value, so that no FP32 cancellation near p = 1 occurs. */
+ * smaller tail probability pt = min(p, 1-p), both formed from the integer
+ * stream value, so that no FP32 cancellation near p = 1 occurs. */
 float lmmo_ppnd7(float q, float pt)
 {
     if (fabsf(q) <= 0.425f) {
@@ -225,10 +227,14 @@ void lmmo_mrg32k3a_normals_f32(uint32_t seed, int64_t first, int64_t count, floa
     mat3 p1 = matpow(A1, (uint64_t)first, M1), p2 = matpow(A2, (uint64_t)first, M2);
     matvec(&p1, x, M1);
     matvec(&p2, y, M2);
+    /* q = u - 1/2 and min(u, 1-u) from the integer stream value, in FP32 */
+    const float normf = (float)(1.0 / 4294967088.0);
     for (int64_t i = 0; i < count; ++i) {
-        const double u = next_u(x, y);
-        const double pt = u < 0.5 ? u : 1.0 - u;
-        z[i] = mean + sd * lmmo_ppnd7((float)(u - 0.5), (float)pt);
+        const uint32_t zi = next_z(x, y);
+        const float q = (float)(int32_t)((int64_t)zi - 2147483544) * normf;
+        const uint32_t zt = zi < 4294967088u - zi ? zi : 4294967088u - zi;
+        const float pt = (float)zt * normf;
+        z[i] = mean + sd * lmmo_ppnd7(q, pt);
     }
 }
 

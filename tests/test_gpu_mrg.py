@@ -1,8 +1,9 @@
 """GPU parity of the MRG32k3a stream (csrc/lmm_mrg.cu) through the C ABI,
 against the oracle's restatement: uniforms bit-exact, normals bit-exact in
-the central branch of AS241 (|u - 1/2| <= 0.425, no log) and within a few
-units in the last place in the tails; the reference-signature calls that
-draw z from this stream."""
+the central branch of AS241 (|u - 1/2| <= 0.425, no log; values within 1e-6
+of the branch boundary are left to the tolerance check, since the FP32 path
+branches on its FP32 q) and within a few units in the last place in the tails;
+the reference-signature calls that draw z from this stream."""
 import numpy as np
 import pytest
 
@@ -68,7 +69,7 @@ def test_normals_f32(first, count, mean, sd):
     g = d.cpu().numpy()
     r = O.mrg32k3a_normals_f32(12345, first, count, mean, sd)
     u = O.mrg32k3a_uniforms(12345, first, count)
-    central = np.abs(u - 0.5) <= 0.425
+    central = np.abs(u - 0.5) <= 0.425 - 1e-6
     np.testing.assert_array_equal(g[central], r[central])
     # the tails go through logf: CUDA's and the host's may differ by an ulp
     np.testing.assert_allclose(g[~central], r[~central], rtol=1e-6, atol=1e-6)
