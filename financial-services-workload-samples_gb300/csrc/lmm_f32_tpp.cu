@@ -4,13 +4,15 @@
 //   forward   path_calc_b1   (LiborMarketModel/liborSwaptionGreeks.cpp:34-82)
 //   payoff    portfolio_b    (:120-211), adjoint aliasing of :178/:181 fixed
 //   reverse   path_calc_b2   (:86-117) plus the vega adjoint (not in the reference)
-// with the NN forward rates L[] and their log-adjoints Pb[] = L*dV/dL held in
-// registers (the rate index is a compile-time register index; the step index
-// is a runtime loop).
+// with the NN inverse forward rates IL[] = 1/L and the log-adjoints
+// Pb[] = L*dV/dL held in registers (the rate index is a compile-time register
+// index; the step index is a runtime loop). Carrying 1/L gives
+// t = L/(1+delta L) = 1/(IL + delta) from one add and one reciprocal, and
+// r = 1/(1+delta L) = 1 - delta t.
 //
 // Branch-free steps. Step n moves rates i > n only. The per-maturity
 // constants are stored with NMAT zero entries in front (k = i-n-1 < 0), so a
-// cell with i <= n multiplies L by 2^0 = 1 and adds 0 to every running sum:
+// cell with i <= n multiplies IL by 2^0 = 1 and adds 0 to every running sum:
 // it is an exact no-op. The forward and the reverse each have ONE unrolled
 // body over the rates, cut into chunks of LMM_TPP_CHUNK rates: a step enters
 // (forward) or leaves (reverse) the body at the chunk holding its first
@@ -20,7 +22,7 @@
 // Reverse sweep without a stored trajectory. With V_i the inclusive drift sum
 // of step n (saved per step by the forward), the Euler step runs backwards,
 // descending in i as the adjoint needs:
-//   L_{n,i} = L_{n+1,i} * 2^-(a_k (V_i + sqez) + c_k),  V_{i-1} = V_i - delta^2 lambda_k t
+//   IL_{n,i} = IL_{n+1,i} * 2^(a_k (V_i + sqez) + c_k),  V_{i-1} = V_i - delta^2 lambda_k t
 // with t = L/(1+delta L), r = 1/(1+delta L). In terms of Pb the reference's
 // update (:108-111) becomes
 //   S += lambda_k Pb_i,   Pb_i += delta^2 lambda_k t r S     (S is the reference's v1)
@@ -95,8 +97,7 @@ struct TppLayout {
     static constexpr int PAD = NMAT;                 // k = i-n-1 >= -NMAT
     static constexpr int NOUT = MODE == Mode::Fused ? 1 + 2 * NN : (MODE == Mode::Forward ? 1 : 2 * NN);
     static constexpr int kc = 0;                                     // float4[PAD+NN]
-    static constexpr int l0 = align16(kc + 16 * (PAD + NN));         // float[NN]
-    static constexpr int il0 = l0 + 4 * NN;                          // float[NN]
+    static constexpr int il0 = align16(kc + 16 * (PAD + NN));        // float[NN]
     static constexpr int ost = il0 + 4 * NN;                         // int[M+1]
     static constexpr int okf = align16(ost + 4 * (M + 1));           // float[kMaxNopt]
     static constexpr int okd = align16(okf + 4 * kMaxNopt);          // double[kMaxNopt]
@@ -136,20 +137,20 @@ __device__ __forceinline__ float4 zquad(const float *zp, uint64_t seed, uint64_t
 // Running drift sum at the start of a step: V = 0, or Y = sqrt(delta) z.
 __device__ __forceinline__ float drift0(float sqez) { return kYrun ? sqez : 0.0f; }
 
-// One forward cell (path_calc_b1 :66-72): drift sum and rate update. k holds
-// the constants of k = i-n-1 (zero for k < 0: an exact no-op).
-__device__ __forceinline__ void fwd_cell(float &L, float &V, const float4 &k, float sqez, float delta)
+// One forward cell (path_calc_b1 :66-72): drift sum and rate update on the
+// inverse rate IL = 1/L. k holds the constants of k = i-n-1 (zero for k < 0:
+// an exact no-op).
+__device__ __forceinline__ void fwd_cell(float &IL, float &V, const float4 &k, float sqez, float delta)
 {
-    const float r = rcp_approx(fmaf(delta, L, 1.0f));
-    V = fmaf(k.z, L * r, V);
-    L *= ex2_approx(fmaf(k.x, kYrun ? V : V + sqez, k.y));
+    V = fmaf(k.z, rcp_approx(IL + delta), V);
+    IL *= ex2_approx(-fmaf(k.x, kYrun ? V : V + sqez, k.y));
 }
 
 // One forward step with a single body: rates are grouped in chunks of CH,
 // and the step starts at the chunk holding its first active rate n+1 (cells
 // of that chunk with i <= n are no-ops). Returns the step's drift sum.
 template <int NN, int CH>
-__device__ __forceinline__ float fwd_step_chunked(float (&L)[NN], const float4 *kcn, float sqez,
+__device__ __forceinline__ float fwd_step_chunked(float (&IL)[NN], const float4 *kcn, float sqez,
                                                   float delta, int n)
 {
     float V = drift0(sqez);
@@ -159,21 +160,21 @@ __device__ __forceinline__ float fwd_step_chunked(float (&L)[NN], const float4 *
         if (c >= c0) {
 #pragma unroll
             for (int i = (c * CH < 1 ? 1 : c * CH); i < (c + 1) * CH && i < NN; ++i)
-                fwd_cell(L[i], V, kcn[i], sqez, delta);
+                fwd_cell(IL[i], V, kcn[i], sqez, delta);
         }
     }
     return V;
 }
 
 // Forward steps n and n+1 with one body over positions p (ascending): cell
-// (n, p) and cell (n+1, p-1). The second finds L_{n+1,p-1} written by cell
+// (n, p) and cell (n+1, p-1). The second finds IL_{n+1,p-1} written by cell
 // (n, p-1) one position earlier, so the two drift chains are independent
 // within a position. Cell (n+1, p-1) has k = p-n-3, the constants loaded for
 // cell (n, p-2), so each constant is loaded once per two cells (ring C[j % 3]).
 // Entered at the chunk holding rate n+1; step n+1's cells below its first
 // active rate n+2 see zero constants and are exact no-ops.
 template <int NN, int CH>
-__device__ __forceinline__ void fwd_pair_window(float (&L)[NN], const float4 *kcn, float sqez0,
+__device__ __forceinline__ void fwd_pair_window(float (&IL)[NN], const float4 *kcn, float sqez0,
                                                 float sqez1, float delta, int n, float &V0, float &V1)
 {
     float4 C[3];
@@ -191,12 +192,12 @@ __device__ __forceinline__ void fwd_pair_window(float (&L)[NN], const float4 *kc
 #pragma unroll
             for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
                 C[p % 3] = kcn[p];
-                if (p >= 1) fwd_cell(L[p], V0, C[p % 3], sqez0, delta);
-                if (p - 1 >= 1) fwd_cell(L[p - 1], V1, C[(p + 1) % 3], sqez1, delta);
+                if (p >= 1) fwd_cell(IL[p], V0, C[p % 3], sqez0, delta);
+                if (p - 1 >= 1) fwd_cell(IL[p - 1], V1, C[(p + 1) % 3], sqez1, delta);
             }
         }
     }
-    fwd_cell(L[NN - 1], V1, C[(NN - 2) % 3], sqez1, delta);
+    fwd_cell(IL[NN - 1], V1, C[(NN - 2) % 3], sqez1, delta);
 }
 
 struct RevStep {
@@ -208,25 +209,24 @@ struct RevStep {
 // One reverse cell (path_calc_b2 :105-111 in log-adjoint form) + vega, with
 // its constants and vega partial sum passed in from the window.
 template <int NN>
-__device__ __forceinline__ void rev_cell(float (&L)[NN], float (&Pb)[NN], RevStep &s, int i,
+__device__ __forceinline__ void rev_cell(float (&IL)[NN], float (&Pb)[NN], RevStep &s, int i,
                                          const float4 &k, float &acc, float delta)
 {
     const float y = kYrun ? s.V : s.V + s.sqez;
-    const float Ln = L[i] * ex2_approx(-fmaf(k.x, y, k.y));
-    const float r = rcp_approx(fmaf(delta, Ln, 1.0f));
-    const float t = Ln * r;
+    const float iln = IL[i] * ex2_approx(fmaf(k.x, y, k.y));
+    const float t = rcp_approx(iln + delta);
     s.V = fmaf(-k.z, t, s.V);
     const float pb = Pb[i];
     s.S = fmaf(k.z, pb, s.S);
     const float tS = t * s.S;
     acc += fmaf(pb, fmaf(-delta, k.w, y), tS);
-    Pb[i] = fmaf(k.w * r, tS, pb);
-    L[i] = Ln;
+    Pb[i] = fmaf(k.w * fmaf(-delta, t, 1.0f), tS, pb);
+    IL[i] = iln;
 }
 
 // Reverse steps n, n-1, ..., n-G+1 with a single body over positions
 // NN-1 .. -(G-1): cell (n-g, i+g) at position i, which finds
-// L_{n-g+1, i+g} written by cell (n-g+1, i+g) one position earlier. With
+// IL_{n-g+1, i+g} written by cell (n-g+1, i+g) one position earlier. With
 // j = i+2g, the constants of cell (n-g, i+g) are st[0].kc[j] and its vega row
 // is st[0].vg[j*B] (k = j-n-1 of step n): C/A hold them from position j
 // (load) to position j-2(G-1) (last use, vega flush), in rings of 2G-1 slots
@@ -238,7 +238,7 @@ __device__ __forceinline__ void rev_cell(float (&L)[NN], float (&Pb)[NN], RevSte
 // position, so leaving there is exact: the rows still open are spare rows
 // (k < 0), which are never read.
 template <int NN, int B, int G, int CH>
-__device__ __forceinline__ void rev_group_window(float (&L)[NN], float (&Pb)[NN], RevStep (&st)[G],
+__device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN], RevStep (&st)[G],
                                                  float delta, int n)
 {
     constexpr int JMAX = NN + G - 2;
@@ -267,7 +267,7 @@ __device__ __forceinline__ void rev_group_window(float (&L)[NN], float (&Pb)[NN]
             for (int g = 0; g < G; ++g) {
                 if (i + g >= 1 && i + g <= NN - 1) {
                     const int j = i + 2 * g;
-                    rev_cell<NN>(L, Pb, st[g], i + g, C[j % W], A[j % W], delta);
+                    rev_cell<NN>(IL, Pb, st[g], i + g, C[j % W], A[j % W], delta);
                 }
             }
             const int jf = i + 2 * (G - 1);
@@ -276,27 +276,33 @@ __device__ __forceinline__ void rev_group_window(float (&L)[NN], float (&Pb)[NN]
     }
 }
 
-// Portfolio value, portfolio_b :133-171 and :186-197. Reciprocals are the
-// correctly rounded FP32 1/(1+delta L); the discount and annuity products,
+// Portfolio value, portfolio_b :133-171 and :186-197, from the inverse rates.
+// The factors 1/(1+delta L) = 1 - delta/(IL + delta) come from correctly
+// rounded FP32 reciprocals (bond_ratio); the discount and annuity products,
 // the annuity sum and the payoffs are FP64. Returns the discounted value;
 // *disc_out receives the discount factor, *mask_out which swaptions (in
 // grouped order) paid, and Bst[m*B] (if given) the annuity factors B[m] of
 // :139 rounded to FP32, for the adjoint.
+__device__ __forceinline__ float bond_ratio(float il, float delta)
+{
+    return fmaf(-delta, __frcp_rn(il + delta), 1.0f);
+}
+
 template <int NN, int NMAT, int B>
-__device__ __forceinline__ double payoff_forward(const float (&L)[NN], float delta, const int *ost,
+__device__ __forceinline__ double payoff_forward(const float (&IL)[NN], float delta, const int *ost,
                                                  const double *oKd, const double *oWd, double *disc_out,
                                                  float *Bst, unsigned long long *mask_out)
 {
     constexpr int M = NN - NMAT;
     double disc = 1.0;
 #pragma unroll
-    for (int n = 0; n < NMAT; ++n) disc *= (double)__frcp_rn(fmaf(delta, L[n], 1.0f));
+    for (int n = 0; n < NMAT; ++n) disc *= (double)bond_ratio(IL[n], delta);
     double b = 1.0, s = 0.0, vs = 0.0;
     unsigned long long mask = 0ull;
     const double dd = (double)delta;
 #pragma unroll
     for (int m = 0; m < M; ++m) {
-        b *= (double)__frcp_rn(fmaf(delta, L[NMAT + m], 1.0f));
+        b *= (double)bond_ratio(IL[NMAT + m], delta);
         s = fma(dd, b, s);
         if (Bst) Bst[m * B] = (float)b;
         const int o1 = ost[m + 1];
@@ -319,7 +325,7 @@ __device__ __forceinline__ double payoff_forward(const float (&L)[NN], float del
 // forward: rebuilding B[m-1] = B[m](1 + delta L) backwards from the last,
 // smallest factor would underflow FP32 on paths whose rates grow large.
 template <int NN, int NMAT, int B>
-__device__ __forceinline__ void payoff_adjoint(const float (&L)[NN], float (&Pb)[NN], float vbar,
+__device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb)[NN], float vbar,
                                                double V, double disc, const float *Bst,
                                                unsigned long long mask, float delta,
                                                const int *ost, const float *oKf, const float *oWf)
@@ -329,8 +335,8 @@ __device__ __forceinline__ void payoff_adjoint(const float (&L)[NN], float (&Pb)
     float Sb = 0.0f, Bb = 0.0f;
 #pragma unroll
     for (int m = M - 1; m >= 0; --m) {
-        const float Ln = L[NMAT + m];
-        const float r = __frcp_rn(fmaf(delta, Ln, 1.0f));
+        const float t = __frcp_rn(IL[NMAT + m] + delta);      // L/(1+delta L)
+        const float r = fmaf(-delta, t, 1.0f);
         const float Bm = Bst[m * B];
         const int o1 = ost[m + 1];
         for (int o = ost[m]; o < o1; ++o) {
@@ -340,14 +346,13 @@ __device__ __forceinline__ void payoff_adjoint(const float (&L)[NN], float (&Pb)
             }
         }
         Bb = fmaf(delta, Sb, Bb);
-        Pb[NMAT + m] = scale * Bb * Bm * (Ln * r);
+        Pb[NMAT + m] = scale * Bb * Bm * t;
         Bb *= r;
     }
     const float vs = -vbar * (float)V * delta;
 #pragma unroll
     for (int n = 0; n < NMAT; ++n) {
-        const float Ln = L[n];
-        Pb[n] = vs * (Ln * __frcp_rn(fmaf(delta, Ln, 1.0f)));
+        Pb[n] = vs * __frcp_rn(IL[n] + delta);
     }
 }
 
@@ -376,7 +381,7 @@ __device__ __forceinline__ void column_reduce(const float *vg, int warp, int lan
 // forward-only kernel runs single steps (the pair's extra live constants
 // cost it more occupancy than they save) and writes the tape.
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
-__device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, float4 &zq,
+__device__ __forceinline__ void forward_all(float (&IL)[NN], const float4 *kc0, float4 &zq,
                                             float4 &zq_next, const float *zp, uint64_t seed,
                                             uint64_t gpath, float sqd, float delta, float *vt_s,
                                             float *tape_v, int64_t total, bool active)
@@ -393,7 +398,7 @@ __device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, f
             const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
             const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
             float V0, V1;
-            fwd_pair_window<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez0, sqez1, delta, n, V0, V1);
+            fwd_pair_window<NN, LMM_TPP_CHUNK>(IL, kc0 - (n + 1), sqez0, sqez1, delta, n, V0, V1);
             vt_s[n * B] = V0;
             vt_s[(n + 1) * B] = V1;
         }
@@ -404,7 +409,7 @@ __device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, f
                 if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
             }
             const float sqez = sqd * pick4(zq, n & 3);
-            const float V = fwd_step_chunked<NN, LMM_TPP_CHUNK>(L, kc0 - (n + 1), sqez, delta, n);
+            const float V = fwd_step_chunked<NN, LMM_TPP_CHUNK>(IL, kc0 - (n + 1), sqez, delta, n);
             if (active) tape_v[(int64_t)n * total] = V;
         }
     }
@@ -412,7 +417,7 @@ __device__ __forceinline__ void forward_all(float (&L)[NN], const float4 *kc0, f
 
 // Reverse over all steps, in groups of G steps from the last.
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
-__device__ __forceinline__ void reverse_all(float (&L)[NN], float (&Pb)[NN], const float4 *kc0,
+__device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], const float4 *kc0,
                                             float *vg0, float4 &zq, float4 &zq_next, const float *zp,
                                             uint64_t seed, uint64_t gpath, float sqd, float delta,
                                             const float *vt_s, const float *tape_v, int64_t total)
@@ -436,7 +441,7 @@ __device__ __forceinline__ void reverse_all(float (&L)[NN], float (&Pb)[NN], con
             st[g].kc = kc0 - (m + 1);
             st[g].vg = vg0 - (m + 1) * B;
         }
-        rev_group_window<NN, B, G, LMM_TPP_CHUNK>(L, Pb, st, delta, n);
+        rev_group_window<NN, B, G, LMM_TPP_CHUNK>(IL, Pb, st, delta, n);
     }
 }
 
@@ -450,7 +455,6 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     static_assert(NMAT % 4 == 0, "normals are read in aligned quads");
     extern __shared__ __align__(16) unsigned char smem[];
     float4 *kc_s = reinterpret_cast<float4 *>(smem + Lay::kc);
-    float *l0_s = reinterpret_cast<float *>(smem + Lay::l0);
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
     float *okf_s = reinterpret_cast<float *>(smem + Lay::okf);
@@ -488,7 +492,6 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         const int scen = unit / w.items, item = unit % w.items;
         __syncthreads();          // the previous unit's reads of l0/il0/acc are done
         for (int i = tid; i < NN; i += B) {
-            l0_s[i] = m.L0f[scen * NN + i];
             il0_s[i] = m.invL0f[scen * NN + i];
         }
         for (int i = tid; i < Lay::NW * 2 * NOUT; i += B) acc_s[i] = 0.0;
@@ -506,37 +509,37 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             const uint64_t gpath = (uint64_t)(path0 + pc);
             float *tape_v = tape ? tape + (int64_t)NN * total + tp : nullptr;
 
-            float L[NN];
+            float IL[NN];
             float Pb[NN];
             float4 zq, zq_next;
 
             if (MODE != Mode::Backward) {
 #pragma unroll
-                for (int i = 0; i < NN; ++i) L[i] = l0_s[i];
+                for (int i = 0; i < NN; ++i) IL[i] = il0_s[i];
                 zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
-                forward_all<NN, NMAT, PHILOX, MODE>(L, kc0, zq, zq_next, zp, seed, gpath, sqd, delta, vt0,
+                forward_all<NN, NMAT, PHILOX, MODE>(IL, kc0, zq, zq_next, zp, seed, gpath, sqd, delta, vt0,
                                                     tape_v, total, active);
                 if (MODE == Mode::Forward && active) {
 #pragma unroll
-                    for (int i = 0; i < NN; ++i) tape[(int64_t)i * total + tp] = L[i];
+                    for (int i = 0; i < NN; ++i) tape[(int64_t)i * total + tp] = IL[i];
                 }
             } else {
 #pragma unroll
-                for (int i = 0; i < NN; ++i) L[i] = tape[(int64_t)i * total + tp];
+                for (int i = 0; i < NN; ++i) IL[i] = tape[(int64_t)i * total + tp];
             }
 
             double disc = 1.0;
             unsigned long long mask = 0ull;
             // B[m] goes to this thread's vega column, unused until the reverse sweep.
             float *Bst = MODE == Mode::Forward ? nullptr : vg0;
-            const double V = payoff_forward<NN, NMAT, B>(L, delta, ost_s, okd_s, owd_s, &disc, Bst, &mask);
+            const double V = payoff_forward<NN, NMAT, B>(IL, delta, ost_s, okd_s, owd_s, &disc, Bst, &mask);
 
             if (MODE != Mode::Forward) {
-                payoff_adjoint<NN, NMAT, B>(L, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s, owf_s);
+                payoff_adjoint<NN, NMAT, B>(IL, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s, owf_s);
 #pragma unroll
                 for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
                 zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);
-                reverse_all<NN, NMAT, PHILOX, MODE>(L, Pb, kc0, vg0, zq, zq_next, zp, seed, gpath, sqd, delta,
+                reverse_all<NN, NMAT, PHILOX, MODE>(IL, Pb, kc0, vg0, zq, zq_next, zp, seed, gpath, sqd, delta,
                                                     vt0, tape_v, total);
             }
 
