@@ -101,4 +101,64 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// Double-FP32 ("float-float") numbers hi + lo, |lo| <= ulp(hi)/2, for the
+// payoff's discount and annuity products and the swap values. They use the
+// error-free transforms TwoSum (Knuth, TAOCP vol. 2, 4.2.2) and the FMA form
+// of Dekker's product, about 48 significant bits. On GB300 an FP64 warp
+// instruction occupies its pipe about as long as 64 FP32 instructions, so
+// these run on the FP32 pipe. Every step is an explicitly rounded intrinsic,
+// so the compiler cannot contract or reorder the error terms.
+struct F2 {
+    float hi, lo;
+};
+
+// a + b as F2, given |a| >= |b| or a == 0 (Fast2Sum).
+__device__ __forceinline__ F2 f2_fast(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ F2 f2_mul(F2 x, float y)
+{
+    const float p = __fmul_rn(x.hi, y);
+    return f2_fast(p, __fmaf_rn(x.lo, y, __fmaf_rn(x.hi, y, -p)));
+}
+
+__device__ __forceinline__ F2 f2_mul(F2 x, F2 y)
+{
+    const float p = __fmul_rn(x.hi, y.hi);
+    float e = __fmaf_rn(x.hi, y.hi, -p);
+    e = __fmaf_rn(x.hi, y.lo, e);
+    e = __fmaf_rn(x.lo, y.hi, e);
+    return f2_fast(p, e);
+}
+
+__device__ __forceinline__ F2 f2_add(F2 x, F2 y)
+{
+    const float s = __fadd_rn(x.hi, y.hi);
+    const float v = __fsub_rn(s, x.hi);
+    const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, v)), __fsub_rn(y.hi, v));
+    return f2_fast(s, __fadd_rn(e, __fadd_rn(x.lo, y.lo)));
+}
+
+__device__ __forceinline__ F2 f2_add(F2 x, float y) { return f2_add(x, F2{y, 0.0f}); }
+
+// The F2 nearest a double (host data staged once per block).
+__device__ __forceinline__ F2 f2_from(double x)
+{
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
+// Swap value (:145) K*s + b - 1 from the F2 annuity sum (sb = s/delta, kd =
+// K*delta) and annuity factor b, rounded once to FP32. For a high part in
+// [1/2, 2] subtracting 1 is exact (Sterbenz); outside it the swap value is
+// far from 0 and one more rounding does not matter.
+__device__ __forceinline__ float f2_swap_value(F2 kd, F2 sb, F2 b)
+{
+    const F2 t = f2_add(f2_mul(sb, kd), b);
+    return __fadd_rn(__fsub_rn(t.hi, 1.0f), t.lo);
+}
+
 }  // namespace lmm

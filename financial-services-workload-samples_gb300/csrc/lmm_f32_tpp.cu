@@ -100,10 +100,9 @@ struct TppLayout {
     static constexpr int il0 = align16(kc + 16 * (PAD + NN));        // float[NN]
     static constexpr int ost = il0 + 4 * NN;                         // int[M+1]
     static constexpr int okf = align16(ost + 4 * (M + 1));           // float[kMaxNopt]
-    static constexpr int okd = align16(okf + 4 * kMaxNopt);          // double[kMaxNopt]
-    static constexpr int owf = align16(okd + 8 * kMaxNopt);          // float[kMaxNopt] weights
-    static constexpr int owd = align16(owf + 4 * kMaxNopt);          // double[kMaxNopt]
-    static constexpr int vt = align16(owd + 8 * kMaxNopt);           // float[NMAT][B]
+    static constexpr int owf = align16(okf + 4 * kMaxNopt);          // float[kMaxNopt] weights
+    static constexpr int okk = align16(owf + 4 * kMaxNopt);          // F2[kMaxNopt]: K delta
+    static constexpr int vt = align16(okk + 8 * kMaxNopt);           // float[NMAT][B]
     static constexpr int vt_bytes = MODE == Mode::Fused ? 4 * NMAT * B : 0;
     static constexpr int vg = vt + vt_bytes;                         // float[PAD+NN][B]
     static constexpr int vg_bytes = MODE == Mode::Forward ? 0 : 4 * (PAD + NN) * B;
@@ -277,46 +276,54 @@ __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN
 }
 
 // Portfolio value, portfolio_b :133-171 and :186-197, from the inverse rates.
-// The factors 1/(1+delta L) = 1 - delta/(IL + delta) come from correctly
-// rounded FP32 reciprocals (bond_ratio); the discount and annuity products,
-// the annuity sum and the payoffs are FP64. Returns the discounted value;
-// *disc_out receives the discount factor, *mask_out which swaptions (in
-// grouped order) paid, and Bst[m*B] (if given) the annuity factors B[m] of
-// :139 rounded to FP32, for the adjoint.
+// The factors 1/(1+delta L) come from t = 1/(IL + delta) (MUFU reciprocal,
+// within 1 ulp) as 1 - delta t while delta L < 1 (within 0.5 + delta L ulp:
+// about 0.5 ulp for ordinary rates) and as IL t above (within 2.5 ulp). The
+// discount and annuity products, the annuity sum, the swap values and the
+// payoff sum are double-FP32 (F2, lmm_device.cuh): FP64-like products on
+// the FP32 pipe (FP64 products cost 10% of the fused kernel's time on
+// GB300). Returns the discounted value; *disc_out receives the discount
+// factor, *mask_out which swaptions (in grouped order) paid, and Bst[m*B] (if
+// given) the annuity factors B[m] of :139 rounded to FP32, for the adjoint.
+__device__ __forceinline__ float bond_ratio_t(float il, float delta, float t)
+{
+    return il > delta ? fmaf(-delta, t, 1.0f) : il * t;
+}
+
 __device__ __forceinline__ float bond_ratio(float il, float delta)
 {
-    return fmaf(-delta, __frcp_rn(il + delta), 1.0f);
+    return bond_ratio_t(il, delta, rcp_approx(il + delta));
 }
 
 template <int NN, int NMAT, int B>
-__device__ __forceinline__ double payoff_forward(const float (&IL)[NN], float delta, const int *ost,
-                                                 const double *oKd, const double *oWd, double *disc_out,
-                                                 float *Bst, unsigned long long *mask_out)
+__device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float delta, const int *ost,
+                                                const F2 *oKd, const float *oWf, float *disc_out,
+                                                float *Bst, unsigned long long *mask_out)
 {
     constexpr int M = NN - NMAT;
-    double disc = 1.0;
+    F2 disc{1.0f, 0.0f};
 #pragma unroll
-    for (int n = 0; n < NMAT; ++n) disc *= (double)bond_ratio(IL[n], delta);
-    double b = 1.0, s = 0.0, vs = 0.0;
+    for (int n = 0; n < NMAT; ++n) disc = f2_mul(disc, bond_ratio(IL[n], delta));
+    F2 b{1.0f, 0.0f}, sb{0.0f, 0.0f}, vs{0.0f, 0.0f};
     unsigned long long mask = 0ull;
-    const double dd = (double)delta;
 #pragma unroll
     for (int m = 0; m < M; ++m) {
-        b *= (double)bond_ratio(IL[NMAT + m], delta);
-        s = fma(dd, b, s);
-        if (Bst) Bst[m * B] = (float)b;
+        b = f2_mul(b, bond_ratio(IL[NMAT + m], delta));
+        sb = f2_add(sb, b);                                   // annuity / delta
+        if (Bst) Bst[m * B] = b.hi;
         const int o1 = ost[m + 1];
         for (int o = ost[m]; o < o1; ++o) {
-            const double sw = fma(oKd[o], s, b) - 1.0;
-            if (sw < 0.0) {
-                vs -= (100.0 * sw) * oWd[o];
+            const float sw = f2_swap_value(oKd[o], sb, b);
+            if (sw < 0.0f) {
+                vs = f2_add(vs, (-100.0f * sw) * oWf[o]);
                 mask |= 1ull << o;
             }
         }
     }
-    *disc_out = disc;
+    *disc_out = disc.hi;
     *mask_out = mask;
-    return disc * vs;
+    const F2 v = f2_mul(vs, disc);
+    return __fadd_rn(v.hi, v.lo);
 }
 
 // Payoff adjoint, portfolio_b :173-184 (with the rate and its adjoint kept
@@ -326,17 +333,17 @@ __device__ __forceinline__ double payoff_forward(const float (&IL)[NN], float de
 // smallest factor would underflow FP32 on paths whose rates grow large.
 template <int NN, int NMAT, int B>
 __device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb)[NN], float vbar,
-                                               double V, double disc, const float *Bst,
+                                               float V, float disc, const float *Bst,
                                                unsigned long long mask, float delta,
                                                const int *ost, const float *oKf, const float *oWf)
 {
     constexpr int M = NN - NMAT;
-    const float scale = -vbar * (float)disc * delta;
+    const float scale = -vbar * disc * delta;
     float Sb = 0.0f, Bb = 0.0f;
 #pragma unroll
     for (int m = M - 1; m >= 0; --m) {
-        const float t = __frcp_rn(IL[NMAT + m] + delta);      // L/(1+delta L)
-        const float r = fmaf(-delta, t, 1.0f);
+        const float t = rcp_approx(IL[NMAT + m] + delta);     // L/(1+delta L)
+        const float r = bond_ratio_t(IL[NMAT + m], delta, t);
         const float Bm = Bst[m * B];
         const int o1 = ost[m + 1];
         for (int o = ost[m]; o < o1; ++o) {
@@ -349,10 +356,10 @@ __device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb
         Pb[NMAT + m] = scale * Bb * Bm * t;
         Bb *= r;
     }
-    const float vs = -vbar * (float)V * delta;
+    const float vs = -vbar * V * delta;
 #pragma unroll
     for (int n = 0; n < NMAT; ++n) {
-        Pb[n] = vs * __frcp_rn(IL[n] + delta);
+        Pb[n] = vs * rcp_approx(IL[n] + delta);
     }
 }
 
@@ -458,9 +465,8 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
     float *okf_s = reinterpret_cast<float *>(smem + Lay::okf);
-    double *okd_s = reinterpret_cast<double *>(smem + Lay::okd);
     float *owf_s = reinterpret_cast<float *>(smem + Lay::owf);
-    double *owd_s = reinterpret_cast<double *>(smem + Lay::owd);
+    F2 *okk_s = reinterpret_cast<F2 *>(smem + Lay::okk);
     float *vt_s = reinterpret_cast<float *>(smem + Lay::vt);
     float *vg_s = reinterpret_cast<float *>(smem + Lay::vg);
     double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
@@ -473,9 +479,8 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     for (int i = tid; i <= M; i += B) ost_s[i] = m.opt_start[i];
     for (int i = tid; i < m.nopt; i += B) {
         okf_s[i] = m.optKf[i];
-        okd_s[i] = m.optKd[i];
         owf_s[i] = m.optWf[i];
-        owd_s[i] = m.optWd[i];
+        okk_s[i] = f2_from(m.optKd[i] * m.deltad);
     }
     double *acc = acc_s + warp * 2 * NOUT;
     const float delta = m.delta, sqd = m.sqd;
@@ -528,11 +533,11 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 for (int i = 0; i < NN; ++i) IL[i] = tape[(int64_t)i * total + tp];
             }
 
-            double disc = 1.0;
+            float disc = 1.0f;
             unsigned long long mask = 0ull;
             // B[m] goes to this thread's vega column, unused until the reverse sweep.
             float *Bst = MODE == Mode::Forward ? nullptr : vg0;
-            const double V = payoff_forward<NN, NMAT, B>(IL, delta, ost_s, okd_s, owd_s, &disc, Bst, &mask);
+            const float V = payoff_forward<NN, NMAT, B>(IL, delta, ost_s, okk_s, owf_s, &disc, Bst, &mask);
 
             if (MODE != Mode::Forward) {
                 payoff_adjoint<NN, NMAT, B>(IL, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s, owf_s);
@@ -545,7 +550,7 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 
             // ---- cross-path reduction of this batch of B paths ----
             if (MODE != Mode::Backward) {
-                const float v = active ? (float)V : 0.0f;
+                const float v = active ? V : 0.0f;
                 const float s1 = warp_sum(v), s2 = warp_sum(v * v);
                 if (lane == 0) {
                     acc[0] += (double)s1;

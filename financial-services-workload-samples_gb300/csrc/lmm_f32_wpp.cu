@@ -20,9 +20,9 @@
 // (Pb = L dV/dL) is
 //   S'_i = delta^2 sum_{j>=i} lambda_k Pb_j,  Pb_i += lambda_k t r S'_i
 //   dV/dlambda_k += Pb_i (Y_i - delta lambda_k) + t S'_i.
-// The payoff (portfolio_b :120-211, aliasing fixed) runs with FP64 products:
-// the discount product is a warp product reduction, the annuity recursion
-// runs on lane 0.
+// The payoff (portfolio_b :120-211, aliasing fixed) runs with double-FP32
+// products and sums (F2, lmm_device.cuh): the discount product is a warp
+// product reduction, the annuity recursion runs on lane 0.
 #include "lmm_device.cuh"
 
 namespace lmm {
@@ -62,7 +62,7 @@ __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(
 // Shared-memory layout (bytes), shared by host and device.
 struct WppLay {
     int nn, nmat, S, nout, M;
-    size_t kc, l0, il0, ost, okf, okd, owf, owd, warp0, per_warp, vg, lw, bw, acc, bytes;
+    size_t kc, l0, il0, ost, okf, owf, okk, warp0, per_warp, vg, lw, bw, acc, bytes;
 };
 
 // Rows in front of the tables: row k + head holds k; rows below head are zero
@@ -83,9 +83,8 @@ __host__ __device__ inline WppLay wpp_layout(int nn, int nmat, int S, Mode mode 
     L.il0 = o; o = al16(o + 4 * (size_t)nn);
     L.ost = o; o = al16(o + 4 * (size_t)(L.M + 1));
     L.okf = o; o = al16(o + 4 * (size_t)kMaxNopt);
-    L.okd = o; o = al16(o + 8 * (size_t)kMaxNopt);
     L.owf = o; o = al16(o + 4 * (size_t)kMaxNopt);    // notional weights
-    L.owd = o; o = al16(o + 8 * (size_t)kMaxNopt);
+    L.okk = o; o = al16(o + 8 * (size_t)kMaxNopt);    // F2 K delta
     L.warp0 = o;
     size_t w = 0;
     L.vg = w; w = al16(w + 4 * (size_t)(32 * S + wpp_head(nmat)));   // head rows discard, then vegas
@@ -249,9 +248,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     float *il0_s = reinterpret_cast<float *>(smem + Ly.il0);
     int *ost_s = reinterpret_cast<int *>(smem + Ly.ost);
     float *okf_s = reinterpret_cast<float *>(smem + Ly.okf);
-    double *okd_s = reinterpret_cast<double *>(smem + Ly.okd);
     float *owf_s = reinterpret_cast<float *>(smem + Ly.owf);
-    double *owd_s = reinterpret_cast<double *>(smem + Ly.owd);
+    F2 *okk_s = reinterpret_cast<F2 *>(smem + Ly.okk);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned char *wbase = smem + Ly.warp0 + warp * Ly.per_warp;
     float *yt = ytop + ((size_t)blockIdx.x * kWppWarps + warp) * wpp_scratch_floats(nmat, S) + lane;
@@ -267,9 +265,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     for (int i = tid; i <= M; i += kWppBlock) ost_s[i] = m.opt_start[i];
     for (int i = tid; i < m.nopt; i += kWppBlock) {
         okf_s[i] = m.optKf[i];
-        okd_s[i] = m.optKd[i];
         owf_s[i] = m.optWf[i];
-        owd_s[i] = m.optWd[i];
+        okk_s[i] = f2_from(m.optKd[i] * m.deltad);
     }
     for (int i = lane; i < 32 * S + head; i += 32) vg_s[i] = 0.0f;
 
@@ -319,41 +316,45 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 const float y = wpp_fwd_step<S>(L, base, n, sqez, lane, kc_s, delta);
                 if (MODE != Mode::Forward) yt[n * 32] = y;
             }
-            // ---- payoff (FP64 products) and its adjoint ----
-            double dprod = 1.0;
+            // ---- payoff (double-FP32 products) and its adjoint ----
+            F2 dprod{1.0f, 0.0f};
 #pragma unroll
             for (int s = 0; s < S; ++s) {
                 const int i = S * lane + s;
-                if (i < nmat) dprod *= (double)__frcp_rn(fmaf(delta, L[s], 1.0f));
+                if (i < nmat) dprod = f2_mul(dprod, __frcp_rn(fmaf(delta, L[s], 1.0f)));
                 if (i < nn) lw_s[i] = L[s];
             }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) dprod *= __shfl_xor_sync(0xffffffffu, dprod, o);
-            const double disc = dprod;
+            for (int o = 16; o > 0; o >>= 1) {
+                const F2 other{__shfl_xor_sync(0xffffffffu, dprod.hi, o), __shfl_xor_sync(0xffffffffu, dprod.lo, o)};
+                dprod = f2_mul(dprod, other);
+            }
+            const float disc = dprod.hi;
             __syncwarp();
-            double V = 0.0;
+            float V = 0.0f;
             if (lane == 0) {
-                double bb = 1.0, ss = 0.0, vs = 0.0;
+                F2 bb{1.0f, 0.0f}, sb{0.0f, 0.0f}, vs{0.0f, 0.0f};
                 unsigned long long mask = 0ull;
                 for (int mm = 0; mm < M; ++mm) {
-                    bb *= (double)__frcp_rn(fmaf(delta, lw_s[nmat + mm], 1.0f));
-                    ss = fma((double)delta, bb, ss);
-                    bw_s[mm] = (float)bb;
+                    bb = f2_mul(bb, __frcp_rn(fmaf(delta, lw_s[nmat + mm], 1.0f)));
+                    sb = f2_add(sb, bb);                      // annuity / delta
+                    bw_s[mm] = bb.hi;
                     for (int o = ost_s[mm]; o < ost_s[mm + 1]; ++o) {
-                        const double sw = fma(okd_s[o], ss, bb) - 1.0;
-                        if (sw < 0.0) {
-                            vs -= (100.0 * sw) * owd_s[o];
+                        const float sw = f2_swap_value(okk_s[o], sb, bb);
+                        if (sw < 0.0f) {
+                            vs = f2_add(vs, (-100.0f * sw) * owf_s[o]);
                             mask |= 1ull << o;
                         }
                     }
                 }
-                V = disc * vs;
+                const F2 v = f2_mul(vs, dprod);
+                V = __fadd_rn(v.hi, v.lo);
                 if (MODE == Mode::Forward) mask = 0ull;     // no adjoint
                 // :173-184 with the rate kept apart from its adjoint; lw_s[i] becomes
                 // the log-adjoint of rate i >= nmat. B[m] comes from the forward
                 // (bw_s): rebuilding it backwards from the last, smallest factor
                 // would underflow FP32 on paths whose rates grow large.
-                const float scale = -vb * (float)disc * delta;
+                const float scale = -vb * disc * delta;
                 float Sb = 0.0f, Bb = 0.0f;
                 for (int mm = M - 1; mm >= 0; --mm) {
                     const float Ln = lw_s[nmat + mm];
@@ -374,12 +375,12 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             __syncwarp();
             if (MODE == Mode::Forward) {
                 if (lane == 0) {
-                    acc[0] += V;
-                    acc[nout] += V * V;
+                    acc[0] += (double)V;
+                    acc[nout] += (double)V * V;
                 }
                 continue;
             }
-            const float vsd = -vb * (float)V * delta;
+            const float vsd = -vb * V * delta;
 #pragma unroll
             for (int s = 0; s < S; ++s) {
                 const int i = S * lane + s;
@@ -401,8 +402,8 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             __syncwarp();
             constexpr int doff = MODE == Mode::Fused ? 1 : 0;   // deltas at doff, vegas at doff + nn
             if (MODE == Mode::Fused && lane == 0) {
-                acc[0] += V;
-                acc[nout] += V * V;
+                acc[0] += (double)V;
+                acc[nout] += (double)V * V;
             }
 #pragma unroll
             for (int s = 0; s < S; ++s) {
