@@ -78,6 +78,17 @@
 #ifndef LMM_TPP_YRUN
 #define LMM_TPP_YRUN 1
 #endif
+// Positions ahead at which the step windows load the constants of a rate
+// from shared memory (0: at the position that first uses them), with the
+// normals read from memory and with Philox normals (more live registers).
+// GB300, 4,194,304 paths: 0 / 1 / 2 ahead: 13.37 / 13.20 / 12.99 ms (HBM
+// normals), 14.00 / 13.62 / 14.17 ms (Philox).
+#ifndef LMM_TPP_PREF
+#define LMM_TPP_PREF 2
+#endif
+#ifndef LMM_TPP_PREF_PHILOX
+#define LMM_TPP_PREF_PHILOX 1
+#endif
 
 
 namespace lmm {
@@ -85,7 +96,12 @@ namespace {
 
 constexpr int kTppBlock = LMM_TPP_BLOCK;
 constexpr int kTppMinBlocks = LMM_TPP_MINB;
+// The forward-only kernel holds no adjoints: 168 registers give it 12 warps
+// per SM.
+constexpr int kTppFwdMinBlocks = 3 * 128 / kTppBlock;
 constexpr bool kYrun = LMM_TPP_YRUN != 0;
+template <bool PHILOX>
+constexpr int kPref = PHILOX ? LMM_TPP_PREF_PHILOX : LMM_TPP_PREF;
 
 __host__ __device__ constexpr int align16(int x) { return (x + 15) & ~15; }
 
@@ -169,14 +185,16 @@ __device__ __forceinline__ float fwd_step_chunked(float (&IL)[NN], const float4 
 // (n, p) and cell (n+1, p-1). The second finds IL_{n+1,p-1} written by cell
 // (n, p-1) one position earlier, so the two drift chains are independent
 // within a position. Cell (n+1, p-1) has k = p-n-3, the constants loaded for
-// cell (n, p-2), so each constant is loaded once per two cells (ring C[j % 3]).
+// cell (n, p-2), so each constant is loaded once per two cells (ring C of
+// 3+P slots, loaded P positions ahead of its first use).
 // Entered at the chunk holding rate n+1; step n+1's cells below its first
 // active rate n+2 see zero constants and are exact no-ops.
-template <int NN, int CH>
+template <int NN, int CH, int P>
 __device__ __forceinline__ void fwd_pair_window(float (&IL)[NN], const float4 *kcn, float sqez0,
                                                 float sqez1, float delta, int n, float &V0, float &V1)
 {
-    float4 C[3];
+    constexpr int R = 3 + P;
+    float4 C[R];
     V0 = drift0(sqez0);
     V1 = drift0(sqez1);
     const int c0 = (n + 1) / CH;
@@ -185,18 +203,18 @@ __device__ __forceinline__ void fwd_pair_window(float (&IL)[NN], const float4 *k
         if (c >= c0) {
             if (c == c0) {
 #pragma unroll
-                for (int j = c * CH - 2; j < c * CH; ++j)
-                    if (j >= 0) C[j % 3] = kcn[j];
+                for (int j = c * CH - 2; j < c * CH + P; ++j)
+                    if (j >= 0 && j < NN) C[j % R] = kcn[j];
             }
 #pragma unroll
             for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
-                C[p % 3] = kcn[p];
-                if (p >= 1) fwd_cell(IL[p], V0, C[p % 3], sqez0, delta);
-                if (p - 1 >= 1) fwd_cell(IL[p - 1], V1, C[(p + 1) % 3], sqez1, delta);
+                if (p + P < NN) C[(p + P) % R] = kcn[p + P];
+                if (p >= 1) fwd_cell(IL[p], V0, C[p % R], sqez0, delta);
+                if (p - 1 >= 1) fwd_cell(IL[p - 1], V1, C[(p + R - 2) % R], sqez1, delta);
             }
         }
     }
-    fwd_cell(IL[NN - 1], V1, C[(NN - 2) % 3], sqez1, delta);
+    fwd_cell(IL[NN - 1], V1, C[(NN - 2) % R], sqez1, delta);
 }
 
 struct RevStep {
@@ -227,29 +245,31 @@ __device__ __forceinline__ void rev_cell(float (&IL)[NN], float (&Pb)[NN], RevSt
 // NN-1 .. -(G-1): cell (n-g, i+g) at position i, which finds
 // IL_{n-g+1, i+g} written by cell (n-g+1, i+g) one position earlier. With
 // j = i+2g, the constants of cell (n-g, i+g) are st[0].kc[j] and its vega row
-// is st[0].vg[j*B] (k = j-n-1 of step n): C/A hold them from position j
-// (load) to position j-2(G-1) (last use, vega flush), in rings of 2G-1 slots
-// indexed j mod (2G-1), so that each constant is loaded once and each vega
-// row gets one read-modify-write per G cells. The body is left at the first
+// is st[0].vg[j*B] (k = j-n-1 of step n): C holds the constants from
+// position j+P (load, P positions ahead of the first use) and A the vega
+// partial sum from position j, both to position j-2(G-1) (last use, vega
+// flush), in rings of 2G-1+P slots indexed j mod (2G-1+P), so that each
+// constant is loaded once and each vega row gets one read-modify-write per
+// G cells. The body is left at the first
 // chunk of CH positions lying wholly below the lowest active position
 // n-2G+3. A vega row is valid (k >= 0) for all or none of its G
 // contributors, and all contributors of a valid row sit at or above that
 // position, so leaving there is exact: the rows still open are spare rows
 // (k < 0), which are never read.
-template <int NN, int B, int G, int CH>
+template <int NN, int B, int G, int CH, int P>
 __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN], RevStep (&st)[G],
                                                  float delta, int n)
 {
     constexpr int JMAX = NN + G - 2;
-    constexpr int W = 2 * G - 1;
+    constexpr int W = 2 * G - 1 + P;
     const float4 *kc = st[0].kc;
     float *vg = st[0].vg;
     float4 C[W];
     float A[W];
 #pragma unroll
-    for (int j = NN; j <= JMAX; ++j) {
+    for (int j = NN - P; j <= JMAX; ++j) {
         C[j % W] = kc[j];
-        A[j % W] = 0.0f;
+        if (j >= NN) A[j % W] = 0.0f;
     }
     const int imin = n - 2 * G + 3;
 #pragma unroll
@@ -258,10 +278,8 @@ __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN
         if (top < imin) return;
 #pragma unroll
         for (int i = top; i > top - CH && i >= -(G - 1); --i) {
-            if (i >= 1) {
-                C[i % W] = kc[i];
-                A[i % W] = 0.0f;
-            }
+            if (i - P >= 1) C[(i - P) % W] = kc[i - P];
+            if (i >= 1) A[i % W] = 0.0f;
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 if (i + g >= 1 && i + g <= NN - 1) {
@@ -405,7 +423,7 @@ __device__ __forceinline__ void forward_all(float (&IL)[NN], const float4 *kc0, 
             const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
             const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
             float V0, V1;
-            fwd_pair_window<NN, LMM_TPP_CHUNK>(IL, kc0 - (n + 1), sqez0, sqez1, delta, n, V0, V1);
+            fwd_pair_window<NN, LMM_TPP_CHUNK, kPref<PHILOX>>(IL, kc0 - (n + 1), sqez0, sqez1, delta, n, V0, V1);
             vt_s[n * B] = V0;
             vt_s[(n + 1) * B] = V1;
         }
@@ -448,12 +466,12 @@ __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], co
             st[g].kc = kc0 - (m + 1);
             st[g].vg = vg0 - (m + 1) * B;
         }
-        rev_group_window<NN, B, G, LMM_TPP_CHUNK>(IL, Pb, st, delta, n);
+        rev_group_window<NN, B, G, LMM_TPP_CHUNK, kPref<PHILOX>>(IL, Pb, st, delta, n);
     }
 }
 
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
-__global__ void __launch_bounds__(kTppBlock, kTppMinBlocks)
+__global__ void __launch_bounds__(kTppBlock, MODE == Mode::Forward ? kTppFwdMinBlocks : kTppMinBlocks)
 k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
       float *__restrict__ tape, const double *__restrict__ vbar)
 {
