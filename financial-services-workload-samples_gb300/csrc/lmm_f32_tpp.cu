@@ -330,6 +330,7 @@ __device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float del
         sb = f2_add(sb, b);                                   // annuity / delta
         if (Bst) Bst[m * B] = b.hi;
         const int o1 = ost[m + 1];
+#pragma unroll 1
         for (int o = ost[m]; o < o1; ++o) {
             const float sw = f2_swap_value(oKd[o], sb, b);
             if (sw < 0.0f) {
@@ -364,6 +365,7 @@ __device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb
         const float r = bond_ratio_t(IL[NMAT + m], delta, t);
         const float Bm = Bst[m * B];
         const int o1 = ost[m + 1];
+#pragma unroll 1
         for (int o = ost[m]; o < o1; ++o) {
             if ((mask >> o) & 1ull) {
                 Sb -= (100.0f * oKf[o]) * oWf[o];
