@@ -121,7 +121,9 @@ struct TppLayout {
     static constexpr int vt = align16(okk + 8 * kMaxNopt);           // float[NMAT][B]
     static constexpr int vt_bytes = MODE == Mode::Fused ? 4 * NMAT * B : 0;
     static constexpr int vg = vt + vt_bytes;                         // float[PAD+NN][B]
-    static constexpr int vg_bytes = MODE == Mode::Forward ? 0 : 4 * (PAD + NN) * B;
+    // Backward/Fused: per-thread vega rows k = -PAD..NN-1; the payoff also
+    // stages the annuity rates there. Forward: only the M staging rows.
+    static constexpr int vg_bytes = MODE == Mode::Forward ? 4 * M * B : 4 * (PAD + NN) * B;
     static constexpr int acc = align16(vg + vg_bytes);               // double[NW][2*NOUT]
     static constexpr int bytes = acc + 8 * NW * 2 * NOUT;
 };
@@ -316,17 +318,22 @@ __device__ __forceinline__ float bond_ratio(float il, float delta)
 template <int NN, int NMAT, int B>
 __device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float delta, const int *ost,
                                                 const F2 *oKd, const float *oWf, float *disc_out,
-                                                float *Bst, unsigned long long *mask_out)
+                                                float *Bst, float *ILst, unsigned long long *mask_out)
 {
     constexpr int M = NN - NMAT;
     F2 disc{1.0f, 0.0f};
 #pragma unroll
     for (int n = 0; n < NMAT; ++n) disc = f2_mul(disc, bond_ratio(IL[n], delta));
+    // The annuity recursion runs as a rolled loop over the rates staged in
+    // shared memory: one copy of its code instead of one per maturity
+    // (instruction cache).
+#pragma unroll
+    for (int m = 0; m < M; ++m) ILst[m * B] = IL[NMAT + m];
     F2 b{1.0f, 0.0f}, sb{0.0f, 0.0f}, vs{0.0f, 0.0f};
     unsigned long long mask = 0ull;
-#pragma unroll
+#pragma unroll 1
     for (int m = 0; m < M; ++m) {
-        b = f2_mul(b, bond_ratio(IL[NMAT + m], delta));
+        b = f2_mul(b, bond_ratio(ILst[m * B], delta));
         sb = f2_add(sb, b);                                   // annuity / delta
         if (Bst) Bst[m * B] = b.hi;
         const int o1 = ost[m + 1];
@@ -352,17 +359,20 @@ __device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float del
 // smallest factor would underflow FP32 on paths whose rates grow large.
 template <int NN, int NMAT, int B>
 __device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb)[NN], float vbar,
-                                               float V, float disc, const float *Bst,
+                                               float V, float disc, const float *Bst, float *ILst,
                                                unsigned long long mask, float delta,
                                                const int *ost, const float *oKf, const float *oWf)
 {
     constexpr int M = NN - NMAT;
     const float scale = -vbar * disc * delta;
     float Sb = 0.0f, Bb = 0.0f;
-#pragma unroll
+    // Rolled over the rates staged by payoff_forward; each staged rate is
+    // replaced by its log-adjoint, copied into Pb[] afterwards.
+#pragma unroll 1
     for (int m = M - 1; m >= 0; --m) {
-        const float t = rcp_approx(IL[NMAT + m] + delta);     // L/(1+delta L)
-        const float r = bond_ratio_t(IL[NMAT + m], delta, t);
+        const float il = ILst[m * B];
+        const float t = rcp_approx(il + delta);               // L/(1+delta L)
+        const float r = bond_ratio_t(il, delta, t);
         const float Bm = Bst[m * B];
         const int o1 = ost[m + 1];
 #pragma unroll 1
@@ -373,9 +383,11 @@ __device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb
             }
         }
         Bb = fmaf(delta, Sb, Bb);
-        Pb[NMAT + m] = scale * Bb * Bm * t;
+        ILst[m * B] = scale * Bb * Bm * t;
         Bb *= r;
     }
+#pragma unroll
+    for (int m = 0; m < M; ++m) Pb[NMAT + m] = ILst[m * B];
     const float vs = -vbar * V * delta;
 #pragma unroll
     for (int n = 0; n < NMAT; ++n) {
@@ -480,6 +492,7 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     using Lay = TppLayout<NN, NMAT, MODE>;
     constexpr int B = Lay::B, M = Lay::M, NOUT = Lay::NOUT, PAD = Lay::PAD;
     static_assert(NMAT % 4 == 0, "normals are read in aligned quads");
+    static_assert(2 * M <= NN, "annuity staging rows inside the vega rows");
     extern __shared__ __align__(16) unsigned char smem[];
     float4 *kc_s = reinterpret_cast<float4 *>(smem + Lay::kc);
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
@@ -557,10 +570,13 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             unsigned long long mask = 0ull;
             // B[m] goes to this thread's vega column, unused until the reverse sweep.
             float *Bst = MODE == Mode::Forward ? nullptr : vg0;
-            const float V = payoff_forward<NN, NMAT, B>(IL, delta, ost_s, okk_s, owf_s, &disc, Bst, &mask);
+            // Staging rows for the annuity rates: vega rows k = M..2M-1 (free
+            // until the reverse sweep), or the forward kernel's own M rows.
+            float *ILst = MODE == Mode::Forward ? vg_s + tid : vg0 + M * B;
+            const float V = payoff_forward<NN, NMAT, B>(IL, delta, ost_s, okk_s, owf_s, &disc, Bst, ILst, &mask);
 
             if (MODE != Mode::Forward) {
-                payoff_adjoint<NN, NMAT, B>(IL, Pb, vb, V, disc, Bst, mask, delta, ost_s, okf_s, owf_s);
+                payoff_adjoint<NN, NMAT, B>(IL, Pb, vb, V, disc, Bst, ILst, mask, delta, ost_s, okf_s, owf_s);
 #pragma unroll
                 for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
                 zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);
