@@ -173,6 +173,39 @@ int f32_family(const lmm_engine *e)
     return 0;
 }
 
+#ifndef LMM_TP2_SHAPES
+#define LMM_TP2_SHAPES 1      // bit 0: nn=160, nmat=120; bit 1: nn=80, nmat=40
+#endif
+
+// Kernel family of an FP32 call: 5 (two threads per path, lmm_f32_tp2.cu)
+// for nn=160, nmat=120, every mode; otherwise f32_family. On GB300 at
+// 160/120 the thread pair runs 2.2x the warp-per-path rate; at 80/40 it runs
+// below the thread-per-path kernel (13.9 vs 11.7 ms at 4,194,304 paths).
+int family_for(const lmm_engine *e, Mode)
+{
+    const bool tp2 = ((LMM_TP2_SHAPES & 1) && e->nn == 160 && e->nmat == 120) ||
+                     ((LMM_TP2_SHAPES & 2) && e->nn == 80 && e->nmat == 40);
+    if (tp2 && lmm::f32_tp2_supports(e->nn, e->nmat)) return 5;
+    return f32_family(e);
+}
+
+// Paths one block takes per batch.
+int batch_paths(int fam)
+{
+    if (fam == 1) return lmm::tpp_block_threads();
+    if (fam == 5) return lmm::tp2_paths_per_block();
+    return lmm::wpp_block_threads() / 32;
+}
+
+cudaError_t launch_f32_family(int fam, const lmm::DevModel &m, Mode mode, const float *z, uint64_t seed,
+                              int64_t path0, bool philox, const Work &w, float *tape, const double *vbar,
+                              cudaStream_t s)
+{
+    if (fam == 1) return lmm::launch_tpp_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
+    if (fam == 5) return lmm::launch_tp2_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
+    return lmm::launch_wpp_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
+}
+
 int blocks_per_sm(lmm_engine *e, int family, Mode mode, bool philox, int *out)
 {
     const int key = variant_key(family, mode, philox);
@@ -185,6 +218,7 @@ int blocks_per_sm(lmm_engine *e, int family, Mode mode, bool philox, int *out)
     cudaError_t err;
     if (family == 1) err = lmm::tpp_blocks_per_sm(mode, philox, &b);
     else if (family == 2) err = lmm::wpp_blocks_per_sm(e->nn, e->nmat, mode, philox, &b);
+    else if (family == 5) err = lmm::tp2_blocks_per_sm(e->nn, e->nmat, mode, philox, &b);
     else if (family == 3) err = lmm::f64_blocks_per_sm(false, &b);
     else err = lmm::f64_blocks_per_sm(true, &b);
     if (err != cudaSuccess) return cuda_fail(err, "occupancy query");
@@ -256,6 +290,15 @@ int wpp_scratch(lmm_engine *e, int64_t blocks, float **out)
     return LMM_OK;
 }
 
+// Scratch of the fused thread-pair kernel for a grid of `blocks` blocks: the
+// forward's drift sums at the half boundary and its rate checkpoints.
+int tp2_scratch(lmm_engine *e, int64_t blocks, float **out)
+{
+    LMM_TRY(e->wscratch.ensure(sizeof(float) * (size_t)blocks * lmm::tp2_scratch_floats_per_block(e->nn, e->nmat)));
+    *out = e->wscratch.as<float>();
+    return LMM_OK;
+}
+
 int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t path0, bool philox,
             int64_t paths, float *tape, const double *d_vbar, double *d_mean, double *d_se)
 {
@@ -263,7 +306,7 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     if (!philox && !d_z) return fail(LMM_ERR_INVALID_ARG, "normals pointer is NULL");
     if (!d_mean) return fail(LMM_ERR_INVALID_ARG, "output pointer is NULL");
     if (philox && (path0 < 0 || path0 > kMaxPaths)) return fail(LMM_ERR_INVALID_ARG, "path0 out of range");
-    const int fam = f32_family(e);
+    const int fam = family_for(e, mode);
     if (fam == 0)
         return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for nn=" + std::to_string(e->nn) +
                                              ", nmat=" + std::to_string(e->nmat));
@@ -272,19 +315,16 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     LMM_TRY(set_device(e));
     int bps = 0;
     LMM_TRY(blocks_per_sm(e, fam, mode, philox, &bps));
-    const int block = fam == 1 ? lmm::tpp_block_threads() : lmm::wpp_block_threads();
     const int nout = mode == Mode::Fused ? 1 + 2 * e->nn : (mode == Mode::Forward ? 1 : 2 * e->nn);
-    // thread-per-path blocks take `block` paths per batch; warp-per-path blocks take block/32.
-    const int per_batch = fam == 1 ? block : block / 32;
+    const int per_batch = batch_paths(fam);
     Work w{};
     LMM_TRY(plan(e, e->nscen, paths, per_batch, bps, nout, &w));
     if (fam == 2) LMM_TRY(wpp_scratch(e, w.grid, &tape));
+    if (fam == 5 && mode == Mode::Fused) LMM_TRY(tp2_scratch(e, w.grid, &tape));
     LMM_TRY(e->flag.ensure(sizeof(int)));
     LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
     mark(e, 0);
-    cudaError_t err = fam == 1
-                          ? lmm::launch_tpp_any(e->dm, mode, d_z, seed, path0, philox, w, tape, d_vbar, e->stream)
-                          : lmm::launch_wpp_any(e->dm, mode, d_z, seed, path0, philox, w, tape, d_vbar, e->stream);
+    cudaError_t err = launch_f32_family(fam, e->dm, mode, d_z, seed, path0, philox, w, tape, d_vbar, e->stream);
     if (err != cudaSuccess) return cuda_fail(err, "FP32 LMM kernel launch");
     mark(e, 1);
     LMM_CK(lmm::launch_finalize(w.partial, e->nscen, w.items, nout, paths, d_mean, d_se,
@@ -782,12 +822,11 @@ constexpr int64_t kPipelineMinPaths = int64_t(1) << 18;
 
 int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
 {
-    const int fam = f32_family(e);
+    const int fam = family_for(e, Mode::Fused);
     if (fam == 0) return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for this shape");
     int bps = 0;
     LMM_TRY(blocks_per_sm(e, fam, Mode::Fused, false, &bps));
-    const int block = fam == 1 ? lmm::tpp_block_threads() : lmm::wpp_block_threads();
-    const int per_batch = fam == 1 ? block : block / 32;
+    const int per_batch = batch_paths(fam);
     const int nout = 1 + 2 * e->nn;
     const int C = kHostChunks;
     int64_t cpaths[kHostChunks], cfirst[kHostChunks], citems[kHostChunks], cppt[kHostChunks];
@@ -803,10 +842,11 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
     }
     LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)total_items * 2 * nout));
     float *wscr = nullptr;
-    if (fam == 2) {
+    if (fam == 2 || fam == 5) {
         int64_t most = 0;
-        for (int c = 0; c < C; ++c) most = std::max(most, citems[c]);
-        LMM_TRY(wpp_scratch(e, most, &wscr));     // the pieces run one after another
+        for (int c = 0; c < C; ++c) most = std::max(most, std::min<int64_t>(citems[c], (int64_t)e->sms * bps));
+        // the pieces run one after another
+        LMM_TRY(fam == 2 ? wpp_scratch(e, most, &wscr) : tp2_scratch(e, most, &wscr));
     }
     LMM_TRY(e->flag.ensure(sizeof(int)));
     if (!e->copy_stream) LMM_CK(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));
@@ -835,9 +875,7 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
         w.grid = (int)std::min<int64_t>(citems[c], (int64_t)e->sms * bps);
         w.partial = part;
         const float *zc = dz + (size_t)cfirst[c] * e->nmat;
-        cudaError_t err = fam == 1
-                              ? lmm::launch_tpp_any(e->dm, Mode::Fused, zc, 0, 0, false, w, nullptr, nullptr, e->stream)
-                              : lmm::launch_wpp_any(e->dm, Mode::Fused, zc, 0, 0, false, w, wscr, nullptr, e->stream);
+        cudaError_t err = launch_f32_family(fam, e->dm, Mode::Fused, zc, 0, 0, false, w, wscr, nullptr, e->stream);
         if (err != cudaSuccess) return cuda_fail(err, "FP32 LMM kernel launch");
         part += (size_t)citems[c] * 2 * nout;
     }
@@ -897,11 +935,16 @@ int lmm_tape_create(lmm_engine *e, int64_t paths, lmm_tape **out)
     std::unique_ptr<lmm_tape> t(new lmm_tape());
     t->e = e;
     t->paths = paths;
-    // The thread-per-path kernels (nn=80, nmat=40) keep the terminal rates and
-    // the per-step drift sums; the warp-per-path backward recomputes its
-    // forward from the same normals and needs no tape.
-    if (f32_family(e) == 1)
-        LMM_TRY(t->buf.ensure(sizeof(float) * (size_t)(e->nn + e->nmat) * e->nscen * (size_t)paths));
+    // The thread-per-path (nn=80, nmat=40) and thread-pair (nn=160, nmat=120)
+    // kernels keep the terminal rates and the per-step drift sums; the
+    // warp-per-path backward recomputes its forward from the same normals and
+    // needs no tape.
+    const int fam = family_for(e, Mode::Forward);
+    if (fam == 1 || fam == 5) {
+        // thread pair: also the drift sums at the half boundary
+        const size_t rows = (size_t)e->nn + (size_t)e->nmat * (fam == 5 ? 2 : 1);
+        LMM_TRY(t->buf.ensure(sizeof(float) * rows * e->nscen * (size_t)paths));
+    }
     *out = t.release();
     return LMM_OK;
 }

@@ -161,4 +161,32 @@ __device__ __forceinline__ float f2_swap_value(F2 kd, F2 sb, F2 b)
     return __fadd_rn(__fsub_rn(t.hi, 1.0f), t.lo);
 }
 
+
+// Four consecutive normals n = 4q..4q+3 of one path: read from memory (16-byte
+// aligned since nmat % 4 == 0) or generated by Philox.
+template <bool PHILOX, int NMAT>
+__device__ __forceinline__ float4 zquad(const float *zp, uint64_t seed, uint64_t gpath, int q)
+{
+    if (PHILOX) {
+        float g[4];
+        normals_quad_f32(seed, gpath, (uint32_t)q, g);
+        return make_float4(g[0], g[1], g[2], g[3]);
+    } else {
+        return __ldg(reinterpret_cast<const float4 *>(zp) + q);
+    }
+}
+
+// The bond ratio 1/(1+delta L) from the inverse rate il = 1/L and
+// t = 1/(il + delta) (MUFU reciprocal, within 1 ulp): 1 - delta t while
+// delta L < 1 (within 0.5 + delta L ulp), il t above (within 2.5 ulp).
+__device__ __forceinline__ float bond_ratio_t(float il, float delta, float t)
+{
+    return il > delta ? fmaf(-delta, t, 1.0f) : il * t;
+}
+
+__device__ __forceinline__ float bond_ratio(float il, float delta)
+{
+    return bond_ratio_t(il, delta, rcp_approx(il + delta));
+}
+
 }  // namespace lmm

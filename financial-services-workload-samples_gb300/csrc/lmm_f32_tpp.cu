@@ -137,20 +137,6 @@ __device__ __forceinline__ float pick4(const float4 &q, int j)
     return r;
 }
 
-// Four consecutive normals n = 4q..4q+3 of one path: read from memory (16-byte
-// aligned since nmat % 4 == 0) or generated by Philox.
-template <bool PHILOX, int NMAT>
-__device__ __forceinline__ float4 zquad(const float *zp, uint64_t seed, uint64_t gpath, int q)
-{
-    if (PHILOX) {
-        float g[4];
-        normals_quad_f32(seed, gpath, (uint32_t)q, g);
-        return make_float4(g[0], g[1], g[2], g[3]);
-    } else {
-        return __ldg(reinterpret_cast<const float4 *>(zp) + q);
-    }
-}
-
 // Running drift sum at the start of a step: V = 0, or Y = sqrt(delta) z.
 __device__ __forceinline__ float drift0(float sqez) { return kYrun ? sqez : 0.0f; }
 
@@ -305,16 +291,6 @@ __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN
 // GB300). Returns the discounted value; *disc_out receives the discount
 // factor, *mask_out which swaptions (in grouped order) paid, and Bst[m*B] (if
 // given) the annuity factors B[m] of :139 rounded to FP32, for the adjoint.
-__device__ __forceinline__ float bond_ratio_t(float il, float delta, float t)
-{
-    return il > delta ? fmaf(-delta, t, 1.0f) : il * t;
-}
-
-__device__ __forceinline__ float bond_ratio(float il, float delta)
-{
-    return bond_ratio_t(il, delta, rcp_approx(il + delta));
-}
-
 template <int NN, int NMAT, int B>
 __device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float delta, const int *ost,
                                                 const F2 *oKd, const float *oWf, float *disc_out,

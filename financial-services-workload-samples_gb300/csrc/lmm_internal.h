@@ -53,6 +53,17 @@ cudaError_t tpp_blocks_per_sm(Mode mode, bool philox, int *blocks);
 cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
                            int64_t path0, bool philox, const Work &w, float *tape,
                            const double *vbar, cudaStream_t s);
+// FP32 kernels with two threads per path (lmm_f32_tp2.cu): nn=160, nmat=120
+// and nn=80, nmat=40; the forward/backward pair keeps the thread-per-path
+// tape layout ([nn][total] terminal inverse rates, [nmat][total] drift sums).
+bool f32_tp2_supports(int nn, int nmat);
+int tp2_paths_per_block();
+// Scratch of the fused kernel per block (floats): the lower half's drift sums
+// at the half boundary per step, and both halves' rate checkpoints.
+size_t tp2_scratch_floats_per_block(int nn, int nmat);
+cudaError_t tp2_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks);
+cudaError_t launch_tp2_any(const DevModel &m, Mode mode, const float *z, uint64_t seed, int64_t path0,
+                           bool philox, const Work &w, float *tape, const double *vbar, cudaStream_t s);
 // FP32 warp-per-path kernels (lmm_f32_wpp.cu, any NN <= kMaxNN; the reverse
 // sweep rebuilds each step from the forward's per-lane drift sums and takes
 // the saved rates every 8 steps).

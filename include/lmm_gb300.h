@@ -149,7 +149,9 @@ int lmm_greeks_philox_device(lmm_engine *e, uint64_t seed, int64_t path0, int64_
 /* The forward/backward split of the fused FP32 call at the payoff, for use as
  * an autograd node. For nn = 80, nmat = 40 the tape holds, per path, the
  * inverse terminal rates 1/L and the per-step drift sums the reverse sweep
- * restarts from: (nn + nmat) floats. For the other shapes (warp-per-path kernels) the
+ * restarts from: (nn + nmat) floats. For nn = 160, nmat = 120 (two threads
+ * per path) it also holds the per-step drift sums at rate nn/2 - 1:
+ * (nn + 2 nmat) floats. For the other shapes (warp-per-path kernels) the
  * backward recomputes the forward from the same normals d_z, and the tape
  * holds no device memory. */
 int lmm_tape_create(lmm_engine *e, int64_t paths, lmm_tape **out);

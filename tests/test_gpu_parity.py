@@ -261,9 +261,9 @@ def _random_cfg(nn, nmat, nopt, seed, paths, vol=(0.1, 0.2)):
 
 @pytest.mark.parametrize("philox", [False, True])
 def test_long_tenor_checkpointed_fp32_matches_oracle(P, philox):
-    """Workload 3 (NN=160, NMAT=120, 30 swaptions): warp-per-path kernel, whose
-    reverse sweep rebuilds each step from the forward's per-lane drift sums and
-    takes the rates saved every 8 steps."""
+    """Workload 3 (NN=160, NMAT=120, 30 swaptions): the two-threads-per-path
+    kernel, whose reverse sweep rebuilds each step from the forward's drift
+    sums at both half tops and takes the rates saved every 8 steps."""
     cfg = cfgs().workload(3, 512)
     seed = 303
     z = O.normals_f32(seed, cfg.paths, cfg.nmat)
@@ -287,9 +287,10 @@ def test_other_shapes_fp32_match_oracle(P, nn, nmat, nopt):
 
 
 @pytest.mark.parametrize("shape", [(160, 120, 3), (33, 7, 2), (200, 100, 4)])
-def test_pair_api_on_warp_per_path_shapes(P, shape):
-    """For shapes other than 80x40 the backward recomputes the forward from the
-    same normals: value and vbar-scaled Greeks equal the fused call's."""
+def test_pair_api_on_other_shapes(P, shape):
+    """160x120 (two threads per path, tape of terminal rates and drift sums)
+    and the warp-per-path shapes (the backward recomputes the forward from the
+    same normals): value and vbar-scaled Greeks equal the fused call's."""
     import torch
     nn, nmat, seed = shape
     cfg = cfgs().workload(3, 256) if nn == 160 else _random_cfg(nn, nmat, 6, seed, 256)
