@@ -39,7 +39,6 @@
 namespace lmm {
 namespace {
 
-constexpr int kTp2Block = 128;     // 4 warps: 2 thread pairs, 64 paths per batch
 constexpr int kTp2Chunk = 8;       // rates per chunk of the step bodies
 constexpr int kTp2Pref = 2;        // constants loaded this many positions ahead
 // The fused kernel saves each half's rates every kTp2Ckpt steps (0: never)
@@ -55,15 +54,24 @@ static_assert(kTp2Ckpt % 2 == 0, "checkpoints fall between step pairs");
 // Rate checkpoints of a fused launch: at times kTp2Ckpt, 2 kTp2Ckpt, ... < nmat.
 __host__ __device__ constexpr int tp2_nckpt(int nmat) { return kTp2Ckpt > 0 ? (nmat - 1) / kTp2Ckpt : 0; }
 
-template <int NN>
-struct Tp2Shape {
-    static constexpr int H = NN / 2;
-    // Resident blocks the registers are sized for: NN=80 holds 40+40 floats
-    // per thread (4 blocks), NN=160 80+80 (2 blocks).
 #ifndef LMM_TP2_MINB40
 #define LMM_TP2_MINB40 4
 #endif
-    static constexpr int kMinBlocks = H <= 40 ? LMM_TP2_MINB40 : 2;
+#ifndef LMM_TP2_WARPS160
+#define LMM_TP2_WARPS160 8
+#endif
+#ifndef LMM_TP2_SWIZZLE
+#define LMM_TP2_SWIZZLE 1
+#endif
+
+template <int NN>
+struct Tp2Shape {
+    static constexpr int H = NN / 2;
+    // Threads per block and resident blocks the registers are sized for:
+    // NN=160 holds 80+80 floats per thread, one block of 8 warps (4 thread
+    // pairs) per SM; NN=80 40+40 floats, 4 blocks of 4 warps.
+    static constexpr int kBlock = 32 * (H <= 40 ? 4 : LMM_TP2_WARPS160);
+    static constexpr int kMinBlocks = H <= 40 ? LMM_TP2_MINB40 : 8 / LMM_TP2_WARPS160;
 };
 
 __host__ __device__ constexpr int al16(int x) { return (x + 15) & ~15; }
@@ -71,7 +79,7 @@ __host__ __device__ constexpr int al16(int x) { return (x + 15) & ~15; }
 template <int NN, int NMAT, Mode MODE>
 struct Tp2Layout {
     static constexpr int H = NN / 2;
-    static constexpr int B = kTp2Block;
+    static constexpr int B = Tp2Shape<NN>::kBlock;
     static constexpr int NP = B / 64;                  // thread pairs per block
     static constexpr int PB = 32 * NP;                 // paths per batch
     static constexpr int M = NN - NMAT;
@@ -222,7 +230,7 @@ __device__ __forceinline__ void tp2_rows_reduce(const float *rows, int lane, dou
 // at rate H-1 of every step [NMAT][total]. Backward: the Greeks of
 // vbar[scen] * value from the tape (payoff rebuilt from the terminal rates).
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
-__global__ void __launch_bounds__(kTp2Block, Tp2Shape<NN>::kMinBlocks)
+__global__ void __launch_bounds__(Tp2Shape<NN>::kBlock, Tp2Shape<NN>::kMinBlocks)
 k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
       float *__restrict__ tape, const double *__restrict__ vbar)
 {
@@ -247,15 +255,18 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int upper = warp & 1, pair = warp >> 1;
+    // Warp w runs on scheduler w % 4. The upper half has the larger share of
+    // the cells (every rate of it is active in steps below H), so warps w
+    // and w + 4 take opposite halves: each scheduler gets one warp of each.
+    const int upper = (warp & 1) ^ (LMM_TP2_SWIZZLE ? (warp >> 2) & 1 : 0), pair = warp >> 1;
     const int ps = pair * 32 + lane;                 // path slot in the batch
     const int base = upper * H;                      // first global rate of this thread
-    for (int i = tid; i < PADK + NN; i += kTp2Block) {
+    for (int i = tid; i < PADK + NN; i += Lay::B) {
         const int k = i - PADK;
         kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
     }
-    for (int i = tid; i <= M; i += kTp2Block) ost_s[i] = m.opt_start[i];
-    for (int i = tid; i < m.nopt; i += kTp2Block) {
+    for (int i = tid; i <= M; i += Lay::B) ost_s[i] = m.opt_start[i];
+    for (int i = tid; i < m.nopt; i += Lay::B) {
         okf_s[i] = m.optKf[i];
         owf_s[i] = m.optWf[i];
         okk_s[i] = f2_from(m.optKd[i] * m.deltad);
@@ -273,8 +284,8 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
         const int scen = unit / w.items, item = unit % w.items;
         __syncthreads();          // the previous unit's reads of il0/acc are done
-        for (int i = tid; i < NN; i += kTp2Block) il0_s[i] = m.invL0f[scen * NN + i];
-        for (int i = tid; i < Lay::NP * 2 * NOUT; i += kTp2Block) acc_s[i] = 0.0;
+        for (int i = tid; i < NN; i += Lay::B) il0_s[i] = m.invL0f[scen * NN + i];
+        for (int i = tid; i < Lay::NP * 2 * NOUT; i += Lay::B) acc_s[i] = 0.0;
         __syncthreads();
 
         const int64_t ibase = (int64_t)item * w.ppt * PB;
@@ -515,7 +526,7 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             __syncthreads();      // vega rows are zeroed by the next batch's payoff
         }
 
-        for (int o = tid; o < 2 * NOUT; o += kTp2Block) {
+        for (int o = tid; o < 2 * NOUT; o += Lay::B) {
             double s = 0.0;
 #pragma unroll
             for (int q = 0; q < Lay::NP; ++q) s += acc_s[q * 2 * NOUT + o];
@@ -533,7 +544,7 @@ cudaError_t launch_tp2(const DevModel &m, const float *z, uint64_t seed, int64_t
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)(w.grid > 0 ? w.grid : (int64_t)m.nscen * w.items);
-    kern<<<grid, kTp2Block, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar);
+    kern<<<grid, Lay::B, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar);
     return cudaGetLastError();
 }
 
@@ -544,18 +555,18 @@ cudaError_t occ_tp2(int *blocks)
     auto kern = k_tp2<NN, NMAT, PHILOX, MODE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, kTp2Block, Lay::bytes);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, Lay::B, Lay::bytes);
 }
 
 }  // namespace
 
 bool f32_tp2_supports(int nn, int nmat) { return (nn == 160 && nmat == 120) || (nn == 80 && nmat == 40); }
 
-int tp2_paths_per_block() { return kTp2Block / 2; }
+int tp2_paths_per_block(int nn) { return nn <= 80 ? Tp2Shape<80>::kBlock / 2 : Tp2Shape<160>::kBlock / 2; }
 
 size_t tp2_scratch_floats_per_block(int nn, int nmat)
 {
-    return (size_t)(nmat + tp2_nckpt(nmat) * nn) * (kTp2Block / 2);
+    return (size_t)(nmat + tp2_nckpt(nmat) * nn) * tp2_paths_per_block(nn);
 }
 
 // Philox normals only in the fused kernel; the pair reads its normals from memory.

@@ -57,7 +57,7 @@ cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_
 // and nn=80, nmat=40; the forward/backward pair keeps the thread-per-path
 // tape layout ([nn][total] terminal inverse rates, [nmat][total] drift sums).
 bool f32_tp2_supports(int nn, int nmat);
-int tp2_paths_per_block();
+int tp2_paths_per_block(int nn);
 // Scratch of the fused kernel per block (floats): the lower half's drift sums
 // at the half boundary per step, and both halves' rate checkpoints.
 size_t tp2_scratch_floats_per_block(int nn, int nmat);
