@@ -173,19 +173,14 @@ int f32_family(const lmm_engine *e)
     return 0;
 }
 
-#ifndef LMM_TP2_SHAPES
-#define LMM_TP2_SHAPES 1      // bit 0: nn=160, nmat=120; bit 1: nn=80, nmat=40
-#endif
-
 // Kernel family of an FP32 call: 5 (two threads per path, lmm_f32_tp2.cu)
 // for nn=160, nmat=120, every mode; otherwise f32_family. On GB300 at
-// 160/120 the thread pair runs 2.2x the warp-per-path rate; at 80/40 it runs
-// below the thread-per-path kernel (13.9 vs 11.7 ms at 4,194,304 paths).
+// 160/120 the thread pair runs 2.1x the warp-per-path rate; at 80/40 it ran
+// 13.4-15.5 ms against 11.7 ms for the thread-per-path kernel (4,194,304
+// paths), so it does not take that shape.
 int family_for(const lmm_engine *e, Mode)
 {
-    const bool tp2 = ((LMM_TP2_SHAPES & 1) && e->nn == 160 && e->nmat == 120) ||
-                     ((LMM_TP2_SHAPES & 2) && e->nn == 80 && e->nmat == 40);
-    if (tp2 && lmm::f32_tp2_supports(e->nn, e->nmat)) return 5;
+    if (lmm::f32_tp2_supports(e->nn, e->nmat)) return 5;
     return f32_family(e);
 }
 

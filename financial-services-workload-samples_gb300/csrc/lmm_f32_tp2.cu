@@ -1,6 +1,6 @@
 // FP32 LMM value + Greeks with two threads per path (a thread pair), for
-// shapes NN = 2H with NMAT >= H: NN=160, NMAT=120 (H = 80) and NN=80,
-// NMAT=40 (H = 40).
+// NN=160, NMAT=120 (H = 80 rates per thread; the code takes any NN = 2H with
+// NMAT >= H).
 //
 // The same Euler cells, payoff and adjoint as the thread-per-path kernel
 // (lmm_f32_tpp.cu; reference LiborMarketModel/liborSwaptionGreeks.cpp
@@ -54,9 +54,6 @@ static_assert(kTp2Ckpt % 2 == 0, "checkpoints fall between step pairs");
 // Rate checkpoints of a fused launch: at times kTp2Ckpt, 2 kTp2Ckpt, ... < nmat.
 __host__ __device__ constexpr int tp2_nckpt(int nmat) { return kTp2Ckpt > 0 ? (nmat - 1) / kTp2Ckpt : 0; }
 
-#ifndef LMM_TP2_MINB40
-#define LMM_TP2_MINB40 4
-#endif
 #ifndef LMM_TP2_WARPS160
 #define LMM_TP2_WARPS160 8
 #endif
@@ -68,10 +65,9 @@ template <int NN>
 struct Tp2Shape {
     static constexpr int H = NN / 2;
     // Threads per block and resident blocks the registers are sized for:
-    // NN=160 holds 80+80 floats per thread, one block of 8 warps (4 thread
-    // pairs) per SM; NN=80 40+40 floats, 4 blocks of 4 warps.
-    static constexpr int kBlock = 32 * (H <= 40 ? 4 : LMM_TP2_WARPS160);
-    static constexpr int kMinBlocks = H <= 40 ? LMM_TP2_MINB40 : 8 / LMM_TP2_WARPS160;
+    // 80+80 floats per thread, one block of 8 warps (4 thread pairs) per SM.
+    static constexpr int kBlock = 32 * LMM_TP2_WARPS160;
+    static constexpr int kMinBlocks = 8 / LMM_TP2_WARPS160;
 };
 
 __host__ __device__ constexpr int al16(int x) { return (x + 15) & ~15; }
@@ -560,9 +556,9 @@ cudaError_t occ_tp2(int *blocks)
 
 }  // namespace
 
-bool f32_tp2_supports(int nn, int nmat) { return (nn == 160 && nmat == 120) || (nn == 80 && nmat == 40); }
+bool f32_tp2_supports(int nn, int nmat) { return nn == 160 && nmat == 120; }
 
-int tp2_paths_per_block(int nn) { return nn <= 80 ? Tp2Shape<80>::kBlock / 2 : Tp2Shape<160>::kBlock / 2; }
+int tp2_paths_per_block(int) { return Tp2Shape<160>::kBlock / 2; }
 
 size_t tp2_scratch_floats_per_block(int nn, int nmat)
 {
@@ -586,7 +582,6 @@ size_t tp2_scratch_floats_per_block(int nn, int nmat)
     do {                                                                                   \
         if (philox && mode != Mode::Fused) return cudaErrorInvalidValue;                   \
         if (nn == 160 && nmat == 120) LMM_TP2_SHAPE(FN, 160, 120, __VA_ARGS__);             \
-        if (nn == 80 && nmat == 40) LMM_TP2_SHAPE(FN, 80, 40, __VA_ARGS__);                \
         return cudaErrorInvalidValue;                                                      \
     } while (0)
 

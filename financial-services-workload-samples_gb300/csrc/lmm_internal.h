@@ -53,9 +53,9 @@ cudaError_t tpp_blocks_per_sm(Mode mode, bool philox, int *blocks);
 cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
                            int64_t path0, bool philox, const Work &w, float *tape,
                            const double *vbar, cudaStream_t s);
-// FP32 kernels with two threads per path (lmm_f32_tp2.cu): nn=160, nmat=120
-// and nn=80, nmat=40; the forward/backward pair keeps the thread-per-path
-// tape layout ([nn][total] terminal inverse rates, [nmat][total] drift sums).
+// FP32 kernels with two threads per path (lmm_f32_tp2.cu): nn=160, nmat=120.
+// The forward/backward pair's tape: [nn][total] terminal inverse rates,
+// [nmat][total] full drift sums, [nmat][total] drift sums at rate nn/2 - 1.
 bool f32_tp2_supports(int nn, int nmat);
 int tp2_paths_per_block(int nn);
 // Scratch of the fused kernel per block (floats): the lower half's drift sums
