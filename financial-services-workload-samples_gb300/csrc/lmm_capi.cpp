@@ -185,9 +185,9 @@ int family_for(const lmm_engine *e, Mode)
 }
 
 // Paths one block takes per batch.
-int batch_paths(const lmm_engine *e, int fam)
+int batch_paths(const lmm_engine *e, int fam, Mode mode)
 {
-    if (fam == 1) return lmm::tpp_block_threads();
+    if (fam == 1) return lmm::tpp_block_threads(mode);
     if (fam == 5) return lmm::tp2_paths_per_block(e->nn);
     return lmm::wpp_block_threads() / 32;
 }
@@ -311,7 +311,7 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     int bps = 0;
     LMM_TRY(blocks_per_sm(e, fam, mode, philox, &bps));
     const int nout = mode == Mode::Fused ? 1 + 2 * e->nn : (mode == Mode::Forward ? 1 : 2 * e->nn);
-    const int per_batch = batch_paths(e, fam);
+    const int per_batch = batch_paths(e, fam, mode);
     Work w{};
     LMM_TRY(plan(e, e->nscen, paths, per_batch, bps, nout, &w));
     if (fam == 2) LMM_TRY(wpp_scratch(e, w.grid, &tape));
@@ -821,7 +821,7 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
     if (fam == 0) return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for this shape");
     int bps = 0;
     LMM_TRY(blocks_per_sm(e, fam, Mode::Fused, false, &bps));
-    const int per_batch = batch_paths(e, fam);
+    const int per_batch = batch_paths(e, fam, Mode::Fused);
     const int nout = 1 + 2 * e->nn;
     const int C = kHostChunks;
     int64_t cpaths[kHostChunks], cfirst[kHostChunks], citems[kHostChunks], cppt[kHostChunks];

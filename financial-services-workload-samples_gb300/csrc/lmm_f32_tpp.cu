@@ -46,13 +46,14 @@
 // fixed order, so results are bit-reproducible.
 #include "lmm_device.cuh"
 
-// 128 threads (4 warps) per block, 2 blocks per SM: 248 registers per thread
-// leave room for 8 warps per SM.
+// Threads per block of the fused kernel: 254 registers per thread leave room
+// for 8 warps per SM, run as one block of 256 threads so that the block
+// barrier keeps all 8 warps on the same stretch of code (GB300, 4,194,304
+// paths: 11.73 ms with two 128-thread blocks per SM, 11.54 ms with one of
+// 256). The forward-only kernel (12 warps per SM) and the backward-only
+// kernel run 128-thread blocks.
 #ifndef LMM_TPP_BLOCK
-#define LMM_TPP_BLOCK 128
-#endif
-#ifndef LMM_TPP_MINB
-#define LMM_TPP_MINB 2
+#define LMM_TPP_BLOCK 256
 #endif
 // Reverse steps processed together as a skewed wavefront (independent
 // reconstruction chains per instruction stream): 2 or 4.
@@ -94,11 +95,12 @@
 namespace lmm {
 namespace {
 
-constexpr int kTppBlock = LMM_TPP_BLOCK;
-constexpr int kTppMinBlocks = LMM_TPP_MINB;
-// The forward-only kernel holds no adjoints: 168 registers give it 12 warps
-// per SM.
-constexpr int kTppFwdMinBlocks = 3 * 128 / kTppBlock;
+template <Mode MODE>
+__host__ __device__ constexpr int tpp_block() { return MODE == Mode::Fused ? LMM_TPP_BLOCK : 128; }
+// Resident blocks the registers are sized for: 8 warps per SM; the
+// forward-only kernel holds no adjoints, and 168 registers give it 12.
+template <Mode MODE>
+__host__ __device__ constexpr int tpp_min_blocks() { return (MODE == Mode::Forward ? 12 : 8) * 32 / tpp_block<MODE>(); }
 constexpr bool kYrun = LMM_TPP_YRUN != 0;
 template <bool PHILOX>
 constexpr int kPref = PHILOX ? LMM_TPP_PREF_PHILOX : LMM_TPP_PREF;
@@ -107,7 +109,7 @@ __host__ __device__ constexpr int align16(int x) { return (x + 15) & ~15; }
 
 template <int NN, int NMAT, Mode MODE>
 struct TppLayout {
-    static constexpr int B = kTppBlock;
+    static constexpr int B = tpp_block<MODE>();
     static constexpr int NW = B / 32;
     static constexpr int M = NN - NMAT;
     static constexpr int PAD = NMAT;                 // k = i-n-1 >= -NMAT
@@ -401,7 +403,7 @@ __device__ __forceinline__ void forward_all(float (&IL)[NN], const float4 *kc0, 
                                             uint64_t gpath, float sqd, float delta, float *vt_s,
                                             float *tape_v, int64_t total, bool active)
 {
-    constexpr int B = kTppBlock;
+    constexpr int B = tpp_block<MODE>();
     if constexpr (MODE == Mode::Fused) {
         static_assert(NMAT % 2 == 0, "paired forward steps");
         for (int n = 0; n < NMAT; n += 2) {
@@ -439,7 +441,7 @@ __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], co
 {
     constexpr int G = LMM_TPP_SKEW;
     static_assert(NMAT % G == 0 && (G == 2 || G == 4), "whole step groups");
-    constexpr int B = kTppBlock;
+    constexpr int B = tpp_block<MODE>();
     for (int n = NMAT - 1; n > 0; n -= G) {
         if (LMM_TPP_SYNC) __syncthreads();
         if ((n & 3) == 3) {
@@ -461,7 +463,7 @@ __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], co
 }
 
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
-__global__ void __launch_bounds__(kTppBlock, MODE == Mode::Forward ? kTppFwdMinBlocks : kTppMinBlocks)
+__global__ void __launch_bounds__(tpp_block<MODE>(), tpp_min_blocks<MODE>())
 k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
       float *__restrict__ tape, const double *__restrict__ vbar)
 {
@@ -607,7 +609,7 @@ cudaError_t launch_tpp(const DevModel &m, const float *z, uint64_t seed, int64_t
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)(w.grid > 0 ? w.grid : (int64_t)m.nscen * w.items);
-    kern<<<grid, kTppBlock, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar);
+    kern<<<grid, Lay::B, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar);
     return cudaGetLastError();
 }
 
@@ -618,14 +620,18 @@ cudaError_t occ_tpp(int *blocks)
     auto kern = k_tpp<NN, NMAT, PHILOX, MODE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, kTppBlock, Lay::bytes);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, Lay::B, Lay::bytes);
 }
 
 }  // namespace
 
 bool f32_tpp_supports(int nn, int nmat) { return nn == 80 && nmat == 40; }
 
-int tpp_block_threads() { return kTppBlock; }
+int tpp_block_threads(Mode mode)
+{
+    return mode == Mode::Fused ? tpp_block<Mode::Fused>()
+                               : (mode == Mode::Forward ? tpp_block<Mode::Forward>() : tpp_block<Mode::Backward>());
+}
 
 #define LMM_TPP_DISPATCH(FN, ...)                                                            \
     do {                                                                                     \

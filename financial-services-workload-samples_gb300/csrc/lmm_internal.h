@@ -48,7 +48,7 @@ enum class Mode : int { Fused = 0, Forward = 1, Backward = 2 };
 
 // FP32 thread-per-path kernels (lmm_f32_tpp.cu, NN=80, NMAT=40).
 bool f32_tpp_supports(int nn, int nmat);
-int tpp_block_threads();
+int tpp_block_threads(Mode mode);     // threads per block = paths per batch
 cudaError_t tpp_blocks_per_sm(Mode mode, bool philox, int *blocks);
 cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
                            int64_t path0, bool philox, const Work &w, float *tape,

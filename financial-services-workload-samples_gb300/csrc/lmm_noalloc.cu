@@ -156,7 +156,7 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
     m.optWd = dmod->owd;
 
     // About two waves of the device, capped by the partial-sum space.
-    const int64_t block = lmm::tpp_block_threads();
+    const int64_t block = lmm::tpp_block_threads(lmm::Mode::Fused);
     const int64_t nscen = p->nscen;
     int64_t items = (2 * (int64_t)ds.sms * ds.bps + nscen - 1) / nscen;
     if (items * nscen > kMaxItems) items = kMaxItems / nscen;
