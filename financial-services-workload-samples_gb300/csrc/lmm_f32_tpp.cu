@@ -50,10 +50,17 @@
 // for 8 warps per SM, run as one block of 256 threads so that the block
 // barrier keeps all 8 warps on the same stretch of code (GB300, 4,194,304
 // paths: 11.73 ms with two 128-thread blocks per SM, 11.54 ms with one of
-// 256). The forward-only kernel (12 warps per SM) and the backward-only
-// kernel run 128-thread blocks.
+// 256). The forward-only kernel (168 registers, 12 warps per SM) runs one
+// block of 384 threads (4.02 -> 3.76 ms against three of 128), the
+// backward-only kernel two blocks of 128 (8.94 ms; one of 256: 9.03 ms).
 #ifndef LMM_TPP_BLOCK
 #define LMM_TPP_BLOCK 256
+#endif
+#ifndef LMM_TPP_BLOCK_FWD
+#define LMM_TPP_BLOCK_FWD 384
+#endif
+#ifndef LMM_TPP_BLOCK_BWD
+#define LMM_TPP_BLOCK_BWD 128
 #endif
 // Reverse steps processed together as a skewed wavefront (independent
 // reconstruction chains per instruction stream): 2 or 4.
@@ -96,7 +103,10 @@ namespace lmm {
 namespace {
 
 template <Mode MODE>
-__host__ __device__ constexpr int tpp_block() { return MODE == Mode::Fused ? LMM_TPP_BLOCK : 128; }
+__host__ __device__ constexpr int tpp_block()
+{
+    return MODE == Mode::Fused ? LMM_TPP_BLOCK : (MODE == Mode::Forward ? LMM_TPP_BLOCK_FWD : LMM_TPP_BLOCK_BWD);
+}
 // Resident blocks the registers are sized for: 8 warps per SM; the
 // forward-only kernel holds no adjoints, and 168 registers give it 12.
 template <Mode MODE>
