@@ -89,10 +89,11 @@
 // Positions ahead at which the step windows load the constants of a rate
 // from shared memory (0: at the position that first uses them), with the
 // normals read from memory and with Philox normals (more live registers).
-// GB300, 4,194,304 paths: 0 / 1 / 2 ahead: 13.37 / 13.20 / 12.99 ms (HBM
-// normals), 14.00 / 13.62 / 14.17 ms (Philox).
+// GB300, one 256-thread block per SM, 4,194,304 paths: 0 / 1 / 2 / 3 ahead:
+// 11.65 / 11.30 / 11.52 / 11.57 ms (HBM normals); 16,777,216 Philox paths:
+// 0 / 1 / 2 ahead: 48.5 / 47.3 / 48.1 ms.
 #ifndef LMM_TPP_PREF
-#define LMM_TPP_PREF 2
+#define LMM_TPP_PREF 1
 #endif
 #ifndef LMM_TPP_PREF_PHILOX
 #define LMM_TPP_PREF_PHILOX 1
