@@ -73,9 +73,15 @@
 #ifndef LMM_TPP_SKEW_BWD
 #define LMM_TPP_SKEW_BWD 2
 #endif
-// Rates per chunk of the single forward and reverse bodies.
+// Rates per chunk of the single forward body, and of the reverse body (a
+// step group leaves it at the first chunk below its lowest active cell).
+// GB300, 4,194,304 paths, fused: reverse chunks of 4 / 8 / 16 rates: 10.98 /
+// 11.09 / 11.41 ms; forward chunks of 4 were slower than 8.
 #ifndef LMM_TPP_CHUNK
 #define LMM_TPP_CHUNK 8
+#endif
+#ifndef LMM_TPP_RCHUNK
+#define LMM_TPP_RCHUNK 4
 #endif
 // 1: carry Y = V + sqrt(delta) z as the running drift sum: one add fewer per
 // cell in each phase (4.6% faster on GB300), at the price of accumulating the
@@ -475,7 +481,7 @@ __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], co
             st[g].kc = kc0 - (m + 1);
             st[g].vg = vg0 - (m + 1) * B;
         }
-        rev_group_window<NN, B, G, LMM_TPP_CHUNK, kPref<PHILOX>>(IL, Pb, st, delta, n);
+        rev_group_window<NN, B, G, LMM_TPP_RCHUNK, kPref<PHILOX>>(IL, Pb, st, delta, n);
     }
 }
 
