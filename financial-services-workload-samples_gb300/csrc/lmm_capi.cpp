@@ -807,9 +807,10 @@ int lmm_swaption_breakdown_f64_device(lmm_engine *e, const double *d_z, int64_t 
 // nothing overlaps, so it is small (1/16: 42 MB of 671 MB at 4M paths, 0.2 ms
 // at the measured 211 GB/s), and each later piece lands before the compute
 // of the pieces ahead of it ends. Measured on GB300 at 4,194,304 paths: 15.8
-// ms per call against 16.4 ms with four equal pieces. Each piece writes its
-// own range of partial sums and one ordered k_finalize covers them all.
-// Single-scenario engines only.
+// ms per call against 16.4 ms with four equal pieces (an earlier kernel);
+// piece boundaries on whole device waves: 363 -> 369 M paths/s. Each piece
+// writes its own range of partial sums and one ordered k_finalize covers them
+// all. Single-scenario engines only.
 constexpr int kHostSplit[] = {1, 3, 6, 6};
 constexpr int kHostChunks = sizeof(kHostSplit) / sizeof(kHostSplit[0]);
 static_assert(kHostChunks <= 8, "one copy event per piece");
@@ -823,14 +824,30 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
     LMM_TRY(blocks_per_sm(e, fam, Mode::Fused, false, &bps));
     const int per_batch = batch_paths(e, fam, Mode::Fused);
     const int nout = 1 + 2 * e->nn;
-    const int C = kHostChunks;
     int64_t cpaths[kHostChunks], cfirst[kHostChunks], citems[kHostChunks], cppt[kHostChunks];
     int64_t total_items = 0, wsum = 0, wcum = 0;
-    for (int c = 0; c < C; ++c) wsum += kHostSplit[c];
+    for (int c = 0; c < kHostChunks; ++c) wsum += kHostSplit[c];
+    // Piece boundaries on whole waves of the device (SMs x resident blocks x
+    // paths per block): every piece but the last runs full waves, so the
+    // pieces together take as many waves as one launch would. Pieces that
+    // round to nothing are dropped.
+    const int64_t wave = (int64_t)e->sms * bps * per_batch;
+    int64_t bnd[kHostChunks + 1];
+    bnd[0] = 0;
+    for (int c = 1; c < kHostChunks; ++c) {
+        wcum += kHostSplit[c - 1];
+        const int64_t x = paths * wcum / wsum;
+        bnd[c] = std::min(std::max((x + wave / 2) / wave * wave, bnd[c - 1]), paths);
+    }
+    bnd[kHostChunks] = paths;
+    int C = 0;
+    for (int c = 0; c < kHostChunks; ++c) {
+        if (bnd[c + 1] <= bnd[c]) continue;
+        cfirst[C] = bnd[c];
+        cpaths[C] = bnd[c + 1] - bnd[c];
+        ++C;
+    }
     for (int c = 0; c < C; ++c) {
-        cfirst[c] = paths * wcum / wsum;
-        wcum += kHostSplit[c];
-        cpaths[c] = paths * wcum / wsum - cfirst[c];
         plan_items(e, 1, cpaths[c], per_batch, bps, &citems[c], &cppt[c]);
         if (cppt[c] > INT32_MAX || citems[c] > INT32_MAX) return fail(LMM_ERR_TOO_LARGE, "launch too large");
         total_items += citems[c];

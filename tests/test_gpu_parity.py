@@ -432,3 +432,23 @@ def test_empty_portfolio_prices_zero(P, nn, nmat):
         g, gse = e.greeks_f32(z)
         g64, _ = e.greeks_f64(z.astype(np.float64))
     assert np.all(g == 0.0) and np.all(gse == 0.0) and np.all(g64 == 0.0)
+
+
+@pytest.mark.parametrize("paths", [300_000, 4_194_304 + 77])
+def test_pipelined_host_call_equals_device_call(P, paths):
+    """The host call above 2^18 paths copies the normals up in pieces on
+    whole waves of the device and launches one kernel per piece: the result
+    equals one device call on the same normals, to FP64 summation order."""
+    import torch
+    cfg = cfgs().workload(2, paths)
+    dz = torch.empty(paths * cfg.nmat, dtype=torch.float32, device="cuda")
+    P.normals_f32_device(61, paths, cfg.nmat, dz.data_ptr())
+    z = dz.cpu().numpy()
+    out = torch.zeros(cfg.nout, dtype=torch.float64, device="cuda")
+    with P.Engine(cfg) as e:
+        e.greeks_f32_device(dz.data_ptr(), paths, out.data_ptr())
+        e.synchronize()
+        g, _ = e.greeks_f32(z, paths)
+        assert e.last_launches >= 3
+    d = out.cpu().numpy()
+    np.testing.assert_allclose(g[0], d, rtol=1e-11, atol=1e-13 * np.abs(d).max())
