@@ -804,14 +804,15 @@ int lmm_swaption_breakdown_f64_device(lmm_engine *e, const double *d_z, int64_t 
 // pieces on the engine's copy stream; the fused kernel of piece c starts as
 // soon as piece c has landed, while the later pieces are still in flight.
 // Relative piece sizes kHostSplit: the first piece's copy is the only one
-// nothing overlaps, so it is small (1/16: 42 MB of 671 MB at 4M paths, 0.2 ms
-// at the measured 211 GB/s), and each later piece lands before the compute
-// of the pieces ahead of it ends. Measured on GB300 at 4,194,304 paths: 15.8
-// ms per call against 16.4 ms with four equal pieces (an earlier kernel);
-// piece boundaries on whole device waves: 363 -> 369 M paths/s. Each piece
-// writes its own range of partial sums and one ordered k_finalize covers them
-// all. Single-scenario engines only.
-constexpr int kHostSplit[] = {1, 3, 6, 6};
+// nothing overlaps, so it is small (1/36: 3 waves, 19 MB of 671 MB at 4M
+// paths, 0.09 ms at the measured 211 GB/s), and each later piece lands
+// before the compute of the pieces ahead of it ends (at 4M paths: 9, 30 and
+// 66 waves). Measured on GB300 at 4,194,304 paths: four equal pieces cost 0.6
+// ms per call more than {1,3,6,6}/16 (an earlier kernel); piece boundaries on
+// whole device waves: 363 -> 369 M paths/s; {1,3,10,22}/36: 369 -> 373 M
+// paths/s. Each piece writes its own range of partial sums and one ordered
+// k_finalize covers them all. Single-scenario engines only.
+constexpr int kHostSplit[] = {1, 3, 10, 22};
 constexpr int kHostChunks = sizeof(kHostSplit) / sizeof(kHostSplit[0]);
 static_assert(kHostChunks <= 8, "one copy event per piece");
 constexpr int64_t kPipelineMinPaths = int64_t(1) << 18;
