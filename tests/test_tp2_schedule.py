@@ -1,0 +1,108 @@
+"""Index arithmetic of the two-threads-per-path kernel (csrc/lmm_f32_tp2.cu),
+replayed on the CPU for NN=160, NMAT=120.
+
+The kernel splits a path's rates between a lower and an upper warp and runs
+the reverse sweep in barrier-separated rounds: in round r the upper half takes
+the step group r and the lower half the group r-1. Each half accumulates vega
+rows of one shared per-path table without atomics, which is correct only if
+the rows the two halves touch in one round are disjoint. These tests enumerate
+every round with the kernel's own window rules (chunked positions, the early
+exit below the lowest active cell, ring flush slots, the final flush of slot 0)
+and check that, and that every constant and vega row the windows address lies
+inside the shared-memory tables (constant rows >= -NMAT, vega rows >= -16).
+"""
+import pytest
+
+NN, NMAT, H = 160, 120, 80
+CH, P, G = 8, 2, 2          # chunk, constant prefetch distance, steps per group
+VPAD, PADK = 16, NMAT       # spare vega rows, zero constant rows in front
+
+
+def rev_window(base, n):
+    """Vega rows (as k) flushed and constant rows (as k) loaded by the reverse
+    window of steps n, n-1 over the half whose first global rate is base."""
+    jmax = H + G - 2
+    imin = n - 1 - base
+    slots, consts = set(), set()
+    if imin >= H:                       # the kernel skips a half with no active cell
+        return set(), set()
+    consts.update(range(H - P, jmax + 1))
+    completed = True
+    q = 0
+    while q * CH < H + G - 1:
+        top = H - 1 - q * CH
+        if top < imin:
+            completed = False
+            break
+        i = top
+        while i > top - CH and i >= -(G - 1):
+            if i - P >= 0:
+                consts.add(i - P)
+            jf = i + 2 * (G - 1)
+            if 0 <= jf <= jmax:
+                slots.add(jf)
+            i -= 1
+        q += 1
+    if completed:
+        slots.add(0)
+    to_k = lambda j: base + j - n - 1
+    return {to_k(j) for j in slots}, {to_k(j) for j in consts}
+
+
+def fwd_window_consts(base, n):
+    """Constant rows (as k) loaded by the forward window of steps n, n+1."""
+    first = n + 1 - base
+    if first >= H:
+        return set()
+    c0 = first // CH if first > 0 else 0
+    consts = {j for j in range(c0 * CH - 2, c0 * CH + P) if j < H}
+    for c in range(c0, H // CH):
+        for p in range(c * CH, (c + 1) * CH):
+            if p + P < H:
+                consts.add(p + P)
+    return {base + j - n - 1 for j in consts}
+
+
+def test_reverse_rounds_touch_disjoint_vega_rows():
+    for r in range(NMAT // 2 + 1):
+        up_rows = low_rows = set()
+        if r < NMAT // 2:
+            up_rows, _ = rev_window(H, NMAT - 1 - 2 * r)
+        if r >= 1:
+            low_rows, _ = rev_window(0, NMAT - 1 - 2 * (r - 1))
+        assert not (up_rows & low_rows), (r, sorted(up_rows & low_rows))
+
+
+@pytest.mark.parametrize("base", [0, H])
+def test_windows_stay_inside_the_tables(base):
+    for n in range(NMAT - 1, 0, -2):
+        rows, consts = rev_window(base, n)
+        assert all(-VPAD <= k <= NN - 1 for k in rows), (base, n, min(rows), max(rows))
+        assert all(-PADK <= k <= NN - 1 for k in consts), (base, n)
+    for n in range(0, NMAT, 2):
+        consts = fwd_window_consts(base, n)
+        assert all(-PADK <= k <= NN - 1 for k in consts), (base, n)
+
+
+def test_every_active_reverse_cell_is_flushed_to_its_own_row():
+    """Each active cell (n', i) of a group adds to row k = i - n' - 1 of its
+    own step; the flushed rows of the two halves together cover all of them."""
+    for g in range(NMAT // 2):
+        n = NMAT - 1 - 2 * g
+        flushed = rev_window(H, n)[0] | rev_window(0, n)[0]
+        for step in (n, n - 1):
+            for i in range(step + 1, NN):
+                assert i - step - 1 in flushed, (n, step, i)
+
+
+def test_forward_hand_over_matches_the_steps_each_half_runs():
+    """Forward round r: the lower half writes the drift sums of steps 2r, 2r+1
+    into buffer r % 2; the upper half reads buffer (r-1) % 2 for steps 2r-2,
+    2r-1, i.e. exactly what the lower half wrote one round earlier, before the
+    lower half overwrites that buffer in round r+1."""
+    written = {}
+    for r in range(NMAT // 2 + 1):
+        if r >= 1:
+            assert written[(r - 1) % 2] == (2 * r - 2, 2 * r - 1)
+        if r < NMAT // 2:
+            written[r % 2] = (2 * r, 2 * r + 1)
