@@ -102,13 +102,13 @@
 // from shared memory (0: at the position that first uses them), with the
 // normals read from memory and with Philox normals (more live registers).
 // GB300, one 256-thread block per SM, 4,194,304 paths: 0 / 1 / 2 / 3 ahead:
-// 11.65 / 11.30 / 11.52 / 11.57 ms (HBM normals); 16,777,216 Philox paths:
-// 0 / 1 / 2 ahead: 48.5 / 47.3 / 48.1 ms.
+// 11.65 / 11.30 / 11.52 / 11.57 ms (HBM normals); 16,777,216 Philox paths
+// with reverse groups of four: 0 / 1 / 2 ahead: 46.02 / 46.13 / 46.79 ms.
 #ifndef LMM_TPP_PREF
 #define LMM_TPP_PREF 1
 #endif
 #ifndef LMM_TPP_PREF_PHILOX
-#define LMM_TPP_PREF_PHILOX 1
+#define LMM_TPP_PREF_PHILOX 0
 #endif
 
 
