@@ -452,3 +452,36 @@ def test_pipelined_host_call_equals_device_call(P, paths):
         assert e.last_launches >= 3
     d = out.cpu().numpy()
     np.testing.assert_allclose(g[0], d, rtol=1e-11, atol=1e-13 * np.abs(d).max())
+
+
+@pytest.mark.parametrize("paths,nscen", [(1, 1), (77, 1), (300, 2)])
+def test_two_threads_per_path_ragged_and_scenarios(P, paths, nscen):
+    """160x120 runs two threads per path in batches of 128 paths: a ragged
+    last batch leaves lanes of both halves idle, and scenarios loop over units
+    of the one-block-per-SM grid. Every scenario matches the FP64 oracle, and
+    the forward/backward pair equals the fused call."""
+    import torch
+    base = cfgs().workload(3, paths)
+    cfg = base.with_paths(paths)
+    if nscen > 1:
+        cfg.L0 = np.stack([base.L0, base.L0 * 1.1])
+    nn = cfg.nn
+    z = O.normals_f32(500 + paths, paths, cfg.nmat)
+    dz = torch.from_numpy(z).cuda()
+    val = torch.zeros(nscen, dtype=torch.float64, device="cuda")
+    grad = torch.zeros(nscen * 2 * nn, dtype=torch.float64, device="cuda")
+    with P.Engine(cfg) as e:
+        g, _ = e.greeks_f32(z)
+        t = e.tape(paths)
+        e.forward_f32_device(dz.data_ptr(), paths, t, val.data_ptr())
+        e.backward_f32_device(dz.data_ptr(), t, [1.0] * nscen, grad.data_ptr())
+        e.synchronize()
+        t.close()
+    v = val.cpu().numpy()
+    gr = grad.cpu().numpy().reshape(nscen, 2 * nn)
+    for s in range(nscen):
+        one = cfg.scenario(s) if nscen > 1 else cfg
+        m, _ = O.greeks(one, z.astype(np.float64))
+        assert_f32_close(g[s], m, nn, f"160x120 {paths} paths scenario {s}")
+        assert v[s] == pytest.approx(g[s][0], rel=1e-12)
+        np.testing.assert_allclose(gr[s], g[s][1:], rtol=2e-6, atol=1e-6 * np.abs(g[s][1:]).max())
