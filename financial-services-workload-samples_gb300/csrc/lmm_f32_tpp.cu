@@ -14,10 +14,11 @@
 // constants are stored with NMAT zero entries in front (k = i-n-1 < 0), so a
 // cell with i <= n multiplies IL by 2^0 = 1 and adds 0 to every running sum:
 // it is an exact no-op. The forward and the reverse each have ONE unrolled
-// body over the rates, cut into chunks of LMM_TPP_CHUNK rates: a step enters
-// (forward) or leaves (reverse) the body at the chunk holding its first
-// active rate, so at most CHUNK-1 no-op cells run per step and the code stays
-// small enough for the instruction cache.
+// body over the rates, cut into chunks (LMM_TPP_CHUNK rates in the forward,
+// LMM_TPP_RCHUNK in the reverse): a step enters (forward) or leaves (reverse)
+// the body at the chunk holding its first active rate, so at most a chunk
+// minus one no-op cells run per step and the code stays small enough for the
+// instruction cache.
 //
 // Reverse sweep without a stored trajectory. With V_i the inclusive drift sum
 // of step n (saved per step by the forward), the Euler step runs backwards,
@@ -33,12 +34,13 @@
 // (k < 0) are NMAT spare rows per thread that are never read.
 // The reconstruction is a serial chain (exp -> rcp -> drift sum) per step, so
 // steps are processed as a skewed wavefront: cell (n,i) next to cell
-// (n-1,i+1), independent chains in one instruction stream. Within such a
-// pair, cell (n-1, i+1) uses the constants and vega row that cell (n, i+2)
-// used two positions earlier; they are kept in registers (rev_group_window),
-// so each constant is read from shared memory once and each vega row gets one
-// read-modify-write per two cells. The fused forward pairs steps the same way
-// (fwd_pair_window).
+// (n-1,i+1), next to (n-2,i+2), ..., G independent chains in one instruction
+// stream (G = LMM_TPP_SKEW = 4 in the fused kernel, LMM_TPP_SKEW_BWD = 2 in
+// the backward-only kernel). Cell (n-g, i+g) uses the constants and vega row
+// that cell (n, i+2g) used 2g positions earlier; they are kept in register
+// rings (rev_group_window), so each constant is read from shared memory once
+// and each vega row gets one read-modify-write per G cells. The fused forward
+// pairs steps the same way (fwd_pair_window).
 //
 // Cross-path reduction: per warp, each lane sums one output column over the
 // warp's 32 paths (shared-memory transpose), then adds into per-warp FP64
