@@ -78,12 +78,27 @@
 // Rates per chunk of the single forward body, and of the reverse body (a
 // step group leaves it at the first chunk below its lowest active cell).
 // GB300, 4,194,304 paths, fused: reverse chunks of 4 / 8 / 16 rates: 10.98 /
-// 11.09 / 11.41 ms; forward chunks of 4 were slower than 8.
+// 11.09 / 11.41 ms, and of 2 see LMM_TPP_FSYNC; forward chunks of 4 were
+// slower than 8.
 #ifndef LMM_TPP_CHUNK
 #define LMM_TPP_CHUNK 8
 #endif
 #ifndef LMM_TPP_RCHUNK
-#define LMM_TPP_RCHUNK 4
+#define LMM_TPP_RCHUNK 2
+#endif
+#ifndef LMM_TPP_RCHUNK_PHILOX
+#define LMM_TPP_RCHUNK_PHILOX 4
+#endif
+// Forward step pairs between block barriers in the fused kernel, with normals
+// from memory and with Philox normals. GB300, 4,194,304 paths: reverse
+// chunks 2 and a barrier every second pair 10.90 -> 10.80 ms; with Philox
+// normals (16.8M paths) the same settings cost 44.22 -> 44.83 ms, so that
+// variant keeps chunks of 4 and a barrier every pair.
+#ifndef LMM_TPP_FSYNC
+#define LMM_TPP_FSYNC 2
+#endif
+#ifndef LMM_TPP_FSYNC_PHILOX
+#define LMM_TPP_FSYNC_PHILOX 1
 #endif
 // 1: carry Y = V + sqrt(delta) z as the running drift sum: one add fewer per
 // cell in each phase (4.6% faster on GB300), at the price of accumulating the
@@ -432,7 +447,7 @@ __device__ __forceinline__ void forward_all(float (&IL)[NN], const float4 *kc0, 
     if constexpr (MODE == Mode::Fused) {
         static_assert(NMAT % 2 == 0, "paired forward steps");
         for (int n = 0; n < NMAT; n += 2) {
-            if (LMM_TPP_SYNC) __syncthreads();
+            if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0) __syncthreads();
             if ((n & 3) == 0) {
                 zq = zq_next;
                 if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
@@ -487,7 +502,8 @@ __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], co
             st[g].kc = kc0 - (m + 1);
             st[g].vg = vg0 - (m + 1) * B;
         }
-        rev_group_window<NN, B, G, LMM_TPP_RCHUNK, kPref<PHILOX>>(IL, Pb, st, delta, n);
+        rev_group_window<NN, B, G, (PHILOX ? LMM_TPP_RCHUNK_PHILOX : LMM_TPP_RCHUNK), kPref<PHILOX>>(IL, Pb, st,
+                                                                                                   delta, n);
     }
 }
 
