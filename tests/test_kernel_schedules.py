@@ -1,5 +1,6 @@
-"""Index arithmetic of the two-threads-per-path kernel (csrc/lmm_f32_tp2.cu),
-replayed on the CPU for NN=160, NMAT=120.
+"""Index arithmetic of the FP32 kernels' reverse windows, replayed on the CPU:
+the two-threads-per-path kernel (csrc/lmm_f32_tp2.cu) for NN=160, NMAT=120,
+and the thread-per-path kernel (csrc/lmm_f32_tpp.cu) for NN=80, NMAT=40.
 
 The kernel splits a path's rates between a lower and an upper warp and runs
 the reverse sweep in barrier-separated rounds: in round r the upper half takes
@@ -106,3 +107,45 @@ def test_forward_hand_over_matches_the_steps_each_half_runs():
             assert written[(r - 1) % 2] == (2 * r - 2, 2 * r - 1)
         if r < NMAT // 2:
             written[r % 2] = (2 * r, 2 * r + 1)
+
+
+# The thread-per-path kernel (csrc/lmm_f32_tpp.cu) leaves its reverse body
+# early in the same way: a group of G steps n, n-1, ..., n-G+1 runs positions
+# from the top in chunks and returns at the first chunk wholly below its
+# lowest active position n - 2G + 3; a vega slot j is flushed (row k = j-n-1)
+# at position j - 2(G-1). Settings as built: fused G = 4 with 2-rate chunks
+# (4 with Philox normals), backward-only G = 2 with 2-rate chunks.
+TPP_NN, TPP_NMAT, TPP_PAD = 80, 40, 40
+
+
+def tpp_rev_window(n, G, ch, p):
+    jmax = TPP_NN + G - 2
+    imin = n - 2 * G + 3
+    flushed, consts = set(), set(range(TPP_NN - p, jmax + 1))
+    q = 0
+    while q * ch < TPP_NN + G - 1:
+        top = TPP_NN - 1 - q * ch
+        if top < imin:
+            break
+        i = top
+        while i > top - ch and i >= -(G - 1):
+            if i - p >= 1:
+                consts.add(i - p)
+            jf = i + 2 * (G - 1)
+            if 1 <= jf <= jmax:
+                flushed.add(jf)
+            i -= 1
+        q += 1
+    return {j - n - 1 for j in flushed}, {j - n - 1 for j in consts}
+
+
+@pytest.mark.parametrize("G,ch,p", [(4, 2, 1), (4, 4, 0), (2, 2, 1)])
+def test_thread_per_path_reverse_windows(G, ch, p):
+    for n in range(TPP_NMAT - 1, 0, -G):
+        rows, consts = tpp_rev_window(n, G, ch, p)
+        assert all(-TPP_PAD <= k <= TPP_NN - 1 for k in rows), (n, min(rows))
+        assert all(-TPP_PAD <= k <= TPP_NN - 1 for k in consts), (n, min(consts))
+        for g in range(G):
+            step = n - g
+            for i in range(step + 1, TPP_NN):
+                assert i - step - 1 in rows, (G, ch, n, step, i)
