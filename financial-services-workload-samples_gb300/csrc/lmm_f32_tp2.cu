@@ -67,7 +67,6 @@ __host__ __device__ constexpr int tp2_nckpt(int nmat) { return kTp2Ckpt > 0 ? (n
 
 template <int NN>
 struct Tp2Shape {
-    static constexpr int H = NN / 2;
     // Threads per block and resident blocks the registers are sized for:
     // 80+80 floats per thread, one block of 8 warps (4 thread pairs) per SM.
     static constexpr int kBlock = 32 * LMM_TP2_WARPS160;
