@@ -49,7 +49,9 @@ class LmmConfig:
     normals: str = "hbm"          # "hbm": pre-generated array; "philox": in-kernel
     seed: int = 1
     ckpt_every: int = 0           # steps between the rate snapshots the reverse sweep
-                                  # restores (warp-per-path kernel); 0: none
+                                  # restores, as the workload names it (descriptive: the
+                                  # 160/120 and warp-per-path kernels save the rates every
+                                  # 8 steps); 0: none
     extra: dict = field(default_factory=dict)
 
     @property
