@@ -2,13 +2,16 @@
 
   oracle/_build/liblmm_oracle.so   the FP64 C restatement (oracle/lmm_oracle.c) and
                                    the MRG32k3a/AS241 stream (oracle/lmm_mrg_oracle.c)
+  oracle/_build/liblmm_cpubase.so  the same sources under reference-like flags
+                                   (fast math, explicit vector target): the
+                                   timed CPU baseline, not the checker
   oracle/_ref/libref_<tag>.so      the UNMODIFIED reference
                                    LiborMarketModel/liborSwaptionGreeks.cpp,
                                    compiled where it lies together with
                                    oracle/ref_harness.cpp and oracle/shim/
 
-The reference builds are only possible where the reference tree is present
-(LMM_REFERENCE_ROOT, default /root/reference); elsewhere they are skipped.
+The reference builds need the reference tree: set LMM_REFERENCE_ROOT to the
+directory that holds LiborMarketModel/. Without it they are skipped.
 Reference shapes other than the default NN=80/NMAT=40 are built against a
 configuration header generated here (same macro names as params.h, other
 values); GCC's -I- makes the reference's quoted #include "params.h" resolve
@@ -27,8 +30,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REF_ROOT = os.environ.get("LMM_REFERENCE_ROOT", "/root/reference")
-LMM_DIR = os.path.join(REF_ROOT, "LiborMarketModel")
+REF_ROOT = os.environ.get("LMM_REFERENCE_ROOT", "")
+LMM_DIR = os.path.join(REF_ROOT, "LiborMarketModel") if REF_ROOT else ""
 
 
 def _cfg_module():
@@ -48,6 +51,29 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
+def _cpu_target_flags():
+    """An explicit target CPU for the timed baseline build (never -march=native,
+    so that what is built is the same wherever the recipe runs): Neoverse V2
+    (the Grace cores) on aarch64, AVX2 on x86-64, as the reference's build
+    targets core-avx2 (LiborMarketModel/compile.sh)."""
+    import platform
+    m = platform.machine().lower()
+    if m in ("aarch64", "arm64"):
+        return ["-mcpu=neoverse-v2"]
+    if m in ("x86_64", "amd64"):
+        return ["-march=x86-64-v3"]
+    return []
+
+
+# The timed CPU baseline: the same source built the way the reference builds
+# its own (LiborMarketModel/compile.sh: -O3, OpenMP, a vector ISA target, the
+# compiler's fast floating-point model with vector math, which icpc applies by
+# default and GCC under -ffast-math). It is timed, never used as the checker:
+# fast math may contract and reorder, so its results are not bitwise the
+# checker's.
+CPUBASE_FLAGS = ["-O3", "-std=c99", "-fopenmp", "-ffast-math", "-fPIC", "-shared", "-w"]
+
+
 def build_oracle(force=False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     srcs = [os.path.join(HERE, "lmm_oracle.c"), os.path.join(HERE, "lmm_mrg_oracle.c")]
@@ -56,6 +82,19 @@ def build_oracle(force=False) -> str:
         tmp = out + f".tmp{os.getpid()}"
         _run(["gcc", "-O3", "-std=c99", "-fopenmp", "-fPIC", "-shared", "-Wall", "-Wextra",
               "-Wno-unused-parameter", *srcs, "-o", tmp, "-lm"])
+        os.replace(tmp, out)
+    return out
+
+
+def build_cpu_baseline(force=False) -> str:
+    """liblmm_cpubase.so: the oracle's source under the reference-like flags
+    (CPUBASE_FLAGS plus an explicit target CPU), for bench.py's timed CPU legs."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = [os.path.join(HERE, "lmm_oracle.c"), os.path.join(HERE, "lmm_mrg_oracle.c")]
+    out = os.path.join(BUILD, "liblmm_cpubase.so")
+    if force or _stale(out, srcs):
+        tmp = out + f".tmp{os.getpid()}"
+        _run(["gcc", *CPUBASE_FLAGS, *_cpu_target_flags(), *srcs, "-o", tmp, "-lm"])
         os.replace(tmp, out)
     return out
 
@@ -105,7 +144,7 @@ def ref_shapes():
 
 def build_reference(force=False) -> dict:
     """Returns {tag: path} for the reference builds; {} without the reference tree."""
-    if not os.path.isfile(os.path.join(LMM_DIR, "liborSwaptionGreeks.cpp")):
+    if not LMM_DIR or not os.path.isfile(os.path.join(LMM_DIR, "liborSwaptionGreeks.cpp")):
         return {}
     os.makedirs(REF_OUT, exist_ok=True)
     harness = os.path.join(HERE, "ref_harness.cpp")
@@ -145,6 +184,7 @@ def build_reference(force=False) -> dict:
 
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
+    print(build_cpu_baseline(force="--force" in sys.argv))
     if "--oracle-only" not in sys.argv:
         for k, v in build_reference(force="--force" in sys.argv).items():
             print(k, v)

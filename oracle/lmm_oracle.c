@@ -207,6 +207,7 @@ static void blk_forward(const lmmo_params *p, const double *z, double *L, double
             const double con1 = d * lam;
             double *Li = L + i * BLK;
             double *Ls = L2 + ((size_t)(n + 1) * nn + i) * BLK;
+#pragma omp simd
             for (int j = 0; j < BLK; ++j) {
                 v[j] += con1 * Li[j] / (1.0 + d * Li[j]);
                 double vrat = exp(con1 * v[j] + lam * (sqez[j] - 0.5 * con1));
@@ -229,6 +230,7 @@ static void blk_payoff(const lmmo_params *p, blk_work *w, double *L, double *v, 
     for (int j = 0; j < BLK; ++j) { b[j] = 1.0; s[j] = 0.0; v[j] = 0.0; }
     for (int m = 0; m < M; ++m) {
         const double *Ln = L + (m + nmat) * BLK;
+#pragma omp simd
         for (int j = 0; j < BLK; ++j) {
             b[j] = b[j] / (1.0 + d * Ln[j]);
             s[j] = s[j] + d * b[j];
@@ -242,6 +244,7 @@ static void blk_payoff(const lmmo_params *p, blk_work *w, double *L, double *v, 
         const int m = p->maturities[o] - 1;
         const double K = p->swaprates[o];
         const double wo = p->weights ? p->weights[o] : 1.0;
+#pragma omp simd
         for (int j = 0; j < BLK; ++j) {
             double swapval = w->B[m * BLK + j] + K * w->S[m * BLK + j] - 1.0;
             if (swapval < 0.0) {
@@ -253,6 +256,7 @@ static void blk_payoff(const lmmo_params *p, blk_work *w, double *L, double *v, 
     }
     for (int m = M - 1; m >= 0; --m) {
         double *Ln = L + (m + nmat) * BLK;
+#pragma omp simd
         for (int j = 0; j < BLK; ++j) {
             w->Bb[m * BLK + j] += d * w->Sb[m * BLK + j];
             if (aliased) {
@@ -314,6 +318,7 @@ static void blk_reverse(const lmmo_params *p, blk_work *w, double *Lb, const dou
             const double *Lp = L2 + ((size_t)(n + 1) * nn + i) * BLK;
             double *Lbi = Lb + i * BLK;
             double *vg = w->vega + (i - n - 1) * BLK;
+#pragma omp simd
             for (int j = 0; j < BLK; ++j) {
                 v1[j] += lam * Lp[j] * Lbi[j];
                 const double faci = d / (1.0 + d * Ln[j]);

@@ -180,12 +180,31 @@ def fd_greeks(cfg, z, paths=None, h=1e-6, threads=0):
     return out
 
 
-def reference_work(cfg, z, paths, threads=0):
-    """The CPU-baseline port: the reference's per-path work (value + delta adjoint)."""
+_cpubase = None
+
+
+def cpubase_lib():
+    """liblmm_cpubase.so: the oracle's source built like the reference's own
+    CPU build (build_ref.CPUBASE_FLAGS); timed, never used as the checker."""
+    global _cpubase
+    if _cpubase is None:
+        L = C.CDLL(build_ref.build_cpu_baseline())
+        L.lmmo_reference_work.argtypes = [C.POINTER(OracleParams), C.POINTER(C.c_double), C.c_int64,
+                                          C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.lmmo_reference_work.restype = C.c_int
+        _cpubase = L
+    return _cpubase
+
+
+def reference_work(cfg, z, paths, threads=0, build="checker"):
+    """The CPU-baseline port: the reference's per-path work (value + delta
+    adjoint). build="checker": the oracle library (portable flags);
+    build="tuned": liblmm_cpubase.so (reference-like flags)."""
     b = _Bound(cfg)
     z = _z64(z)
     v, d = C.c_double(), C.c_double()
-    rc = lib().lmmo_reference_work(C.byref(b.p), _dp(z), paths, threads, C.byref(v), C.byref(d))
+    L = cpubase_lib() if build == "tuned" else lib()
+    rc = L.lmmo_reference_work(C.byref(b.p), _dp(z), paths, threads, C.byref(v), C.byref(d))
     if rc:
         raise RuntimeError(f"lmmo_reference_work failed ({rc})")
     return v.value, d.value

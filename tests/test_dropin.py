@@ -1,8 +1,9 @@
 """The drop-in claim: the reference's own driver (LiborMarketModel/main.cpp,
 unmodified) compiles and links against this library with the shim
 (shim/liborSwaptionGreeks_gb300.cpp) replacing liborSwaptionGreeks.cpp and
-mklRng.cpp, in the FP64 and FP32 builds. Where the reference tree is absent
-(the GPU machine) there is nothing to link and the test is skipped."""
+mklRng.cpp, in the FP64 and FP32 builds. The reference tree is named by
+LMM_REFERENCE_ROOT; without it there is nothing to link and the test is
+skipped."""
 import os
 import subprocess
 
@@ -10,13 +11,13 @@ import pytest
 
 from conftest import ROOT, pkg
 
-REF = os.environ.get("LMM_REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("LMM_REFERENCE_ROOT", "")
 
 
 @pytest.mark.parametrize("double", [True, False])
 def test_reference_driver_links_against_the_library(tmp_path, double):
-    if not os.path.isfile(os.path.join(REF, "LiborMarketModel", "main.cpp")):
-        pytest.skip("reference tree not present")
+    if not REF or not os.path.isfile(os.path.join(REF, "LiborMarketModel", "main.cpp")):
+        pytest.skip("LMM_REFERENCE_ROOT does not name the reference tree")
     P = pkg()
     if not os.path.exists(P.LIB_PATH):
         P.build()
