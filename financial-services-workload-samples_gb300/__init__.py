@@ -36,7 +36,8 @@ EXPORTS = (
     "lmm_mrg32k3a_uniforms_device", "lmm_mrg32k3a_normals_f64_device", "lmm_mrg32k3a_normals_f32_device",
     "lmm_swaption_greeks_mrg32k3a", "lmm_swaption_greeks_mrg32k3a_f32",
     "lmm_engine_set_weights", "lmm_swaption_breakdown_f32_device", "lmm_swaption_breakdown_f64_device",
-    "lmm_mufu_peak_gops", "lmm_fp64_peak_tflops",
+    "lmm_mufu_peak_gops", "lmm_fp64_peak_tflops", "lmm_engine_set_checkpoint_interval",
+    "lmm_engine_checkpoint_interval",
 )
 
 
@@ -106,6 +107,8 @@ def lib():
         "lmm_swaption_greeks_f32": ([fp, C.c_int, C.c_float, C.c_float, C.c_int, fp, fp, C.c_int], C.c_int),
         "lmm_greeks_f32_device_noalloc": ([P, vp, i64, vp, vp, vp], C.c_int),
         "lmm_engine_set_weights": ([vp, dp], C.c_int),
+        "lmm_engine_set_checkpoint_interval": ([vp, i32], C.c_int),
+        "lmm_engine_checkpoint_interval": ([vp], i32),
         "lmm_swaption_breakdown_f32_device": ([vp, vp, i64, vp, vp], C.c_int),
         "lmm_swaption_breakdown_f64_device": ([vp, vp, i64, vp, vp], C.c_int),
         "lmm_mrg32k3a_uniforms_device": ([C.c_uint32, i64, i64, vp, vp], C.c_int),
@@ -175,6 +178,8 @@ class Engine:
         h = C.c_void_p()
         _check(lib().lmm_engine_create(C.byref(self._ref.p), device, C.byref(h)), "lmm_engine_create")
         self.h = h
+        if getattr(cfg, "ckpt_every", None) is not None:
+            self.set_checkpoint_interval(cfg.ckpt_every)
 
     def close(self):
         if getattr(self, "h", None):
@@ -198,6 +203,14 @@ class Engine:
 
     def synchronize(self):
         _check(lib().lmm_engine_synchronize(self.h), "lmm_engine_synchronize")
+
+    def set_checkpoint_interval(self, steps: int):
+        """Steps between the rate checkpoints of the FP32 reverse sweep (0: none)."""
+        _check(lib().lmm_engine_set_checkpoint_interval(self.h, int(steps)), "lmm_engine_set_checkpoint_interval")
+
+    @property
+    def checkpoint_interval(self) -> int:
+        return int(lib().lmm_engine_checkpoint_interval(self.h))
 
     @property
     def last_launches(self) -> int:

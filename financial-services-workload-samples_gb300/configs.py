@@ -48,10 +48,10 @@ class LmmConfig:
     paths: int
     normals: str = "hbm"          # "hbm": pre-generated array; "philox": in-kernel
     seed: int = 1
-    ckpt_every: int = 0           # steps between the rate snapshots the reverse sweep
-                                  # restores, as the workload names it (descriptive: the
-                                  # 160/120 and warp-per-path kernels save the rates every
-                                  # 8 steps); 0: none
+    ckpt_every: int | None = None  # steps between the rate checkpoints the FP32 reverse
+                                   # sweep restores (Engine applies it through
+                                   # lmm_engine_set_checkpoint_interval); 0: none; None:
+                                   # the engine's default (8, and none at 80/40)
     extra: dict = field(default_factory=dict)
 
     @property

@@ -43,6 +43,15 @@ int cuda_fail(cudaError_t e, const char *what)
     return LMM_ERR_CUDA;
 }
 
+}  // namespace
+
+namespace lmm {
+int record_error(int status, const char *what) { return fail(status, what); }
+int record_cuda_error(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+}  // namespace lmm
+
+namespace {
+
 #define LMM_CK(call)                                         \
     do {                                                     \
         cudaError_t lmm_e_ = (call);                         \
@@ -84,6 +93,9 @@ struct DevBuf {
 };
 
 constexpr int64_t kMaxPaths = int64_t(1) << 40;
+// Steps between the rate checkpoints of the long-tenor FP32 reverse sweeps
+// when the caller sets none (the 160/120 workload's interval).
+constexpr int kDefaultCkpt = 8;
 
 }  // namespace
 
@@ -280,7 +292,7 @@ int check_paths(int64_t paths)
 int wpp_scratch(lmm_engine *e, int64_t blocks, float **out)
 {
     const size_t warps = (size_t)blocks * (lmm::wpp_block_threads() / 32);
-    LMM_TRY(e->wscratch.ensure(sizeof(float) * warps * lmm::wpp_scratch_floats_per_warp(e->nn, e->nmat)));
+    LMM_TRY(e->wscratch.ensure(sizeof(float) * warps * lmm::wpp_scratch_floats_per_warp(e->nn, e->nmat, e->dm.ckpt)));
     *out = e->wscratch.as<float>();
     return LMM_OK;
 }
@@ -289,7 +301,8 @@ int wpp_scratch(lmm_engine *e, int64_t blocks, float **out)
 // forward's drift sums at the half boundary and its rate checkpoints.
 int tp2_scratch(lmm_engine *e, int64_t blocks, float **out)
 {
-    LMM_TRY(e->wscratch.ensure(sizeof(float) * (size_t)blocks * lmm::tp2_scratch_floats_per_block(e->nn, e->nmat)));
+    LMM_TRY(e->wscratch.ensure(sizeof(float) * (size_t)blocks *
+                               lmm::tp2_scratch_floats_per_block(e->nn, e->nmat, e->dm.ckpt)));
     *out = e->wscratch.as<float>();
     return LMM_OK;
 }
@@ -558,6 +571,9 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
     m.optKd = reinterpret_cast<const double *>(base + o_okd);
     m.optWf = e->wf_rows;
     m.optWd = e->wd_rows;
+    // The long-tenor kernels restore saved rates every kDefaultCkpt steps;
+    // the thread-per-path kernel (80/40) takes no rate checkpoints.
+    m.ckpt = lmm::f32_tpp_supports(nn, nmat) ? 0 : kDefaultCkpt;
 
     LMM_CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
     e->own_stream = true;
@@ -592,6 +608,26 @@ int lmm_engine_destroy(lmm_engine *e)
     delete e;
     return LMM_OK;
 }
+
+int lmm_engine_set_checkpoint_interval(lmm_engine *e, int32_t steps)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    if (steps < 0 || steps > e->nmat) return fail(LMM_ERR_INVALID_ARG, "steps must be in [0, nmat]");
+    const int fam = family_for(e, Mode::Fused);
+    if (fam == 0)
+        return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for nn=" + std::to_string(e->nn) +
+                                             ", nmat=" + std::to_string(e->nmat));
+    if (fam == 1 && steps != 0)
+        return fail(LMM_ERR_UNSUPPORTED, "the nn=80, nmat=40 kernel keeps every step's drift sums on chip and "
+                                         "takes no rate checkpoints: only 0 is accepted");
+    if (fam == 5 && steps % 2 != 0)
+        return fail(LMM_ERR_UNSUPPORTED, "the nn=160, nmat=120 kernel runs its steps in pairs: the interval "
+                                         "must be even");
+    e->dm.ckpt = steps;
+    return LMM_OK;
+}
+
+int32_t lmm_engine_checkpoint_interval(const lmm_engine *e) { return e ? e->dm.ckpt : -1; }
 
 int lmm_engine_set_stream(lmm_engine *e, void *stream)
 {

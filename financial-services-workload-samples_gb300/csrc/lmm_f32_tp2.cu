@@ -41,18 +41,12 @@ namespace {
 
 constexpr int kTp2Chunk = 8;       // rates per chunk of the step bodies
 constexpr int kTp2Pref = 2;        // constants loaded this many positions ahead
-// The fused kernel saves each half's rates every kTp2Ckpt steps (0: never)
-// and the reverse sweep takes them in place of its rebuilt rates there, so
-// FP32 rounding of the backward Euler steps accumulates over at most
-// kTp2Ckpt steps.
-#ifndef LMM_TP2_CKPT
-#define LMM_TP2_CKPT 8
-#endif
-constexpr int kTp2Ckpt = LMM_TP2_CKPT;
-static_assert(kTp2Ckpt % 2 == 0, "checkpoints fall between step pairs");
-
-// Rate checkpoints of a fused launch: at times kTp2Ckpt, 2 kTp2Ckpt, ... < nmat.
-__host__ __device__ constexpr int tp2_nckpt(int nmat) { return kTp2Ckpt > 0 ? (nmat - 1) / kTp2Ckpt : 0; }
+// The fused kernel saves each half's rates every ck = DevModel::ckpt steps
+// (0: never; ck even, so that checkpoints fall between step pairs) and the
+// reverse sweep takes them in place of its rebuilt rates there, so FP32
+// rounding of the backward Euler steps accumulates over at most ck steps.
+// Rate checkpoints of a fused launch: at times ck, 2 ck, ... < nmat.
+__host__ __device__ constexpr int tp2_nckpt(int nmat, int ck) { return ck > 0 ? (nmat - 1) / ck : 0; }
 
 // Warps per block (8: one block per SM; 4: two blocks per SM), and whether
 // warps w and w+4, which share a scheduler, take opposite halves (1) or the
@@ -224,7 +218,7 @@ __device__ __forceinline__ void tp2_rows_reduce(const float *rows, int lane, dou
 }
 
 // MODE Fused: value + Greeks; `tape` is the launch's scratch: [grid][NMAT][PB]
-// drift sums at rate H-1, then [grid][tp2_nckpt][NN][PB] rate checkpoints. Forward: value, and the tape: terminal inverse rates
+// drift sums at rate H-1, then [grid][tp2_nckpt][NN][PB] rate checkpoints, one every m.ckpt steps. Forward: value, and the tape: terminal inverse rates
 // [NN][total], the full drift sum of every step [NMAT][total], the drift sum
 // at rate H-1 of every step [NMAT][total]. Backward: the Greeks of
 // vbar[scen] * value from the tape (payoff rebuilt from the terminal rates).
@@ -300,8 +294,9 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             float *tape_v = MODE == Mode::Fused ? nullptr : tape + (int64_t)NN * total + tp;
             float *hsum = MODE == Mode::Fused ? tape + (int64_t)blockIdx.x * NMAT * PB + ps
                                               : tape + (int64_t)(NN + NMAT) * total + tp;
-            constexpr int NCK = MODE == Mode::Fused ? tp2_nckpt(NMAT) : 0;
-            // checkpoint c (the rates after step (c+1) kTp2Ckpt - 1), local rate i: ckp[(c*NN + i)*PB]
+            const int ck = MODE == Mode::Fused ? m.ckpt : 0;
+            const int NCK = tp2_nckpt(NMAT, ck);
+            // checkpoint c (the rates after step (c+1) ck - 1), local rate i: ckp[(c*NN + i)*PB]
             float *ckp = tape + (int64_t)gridDim.x * NMAT * PB + (int64_t)blockIdx.x * NCK * NN * PB + base * PB + ps;
 
             float X[H];
@@ -350,9 +345,9 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                         tape_v[(int64_t)n * total] = Y0;
                         tape_v[(int64_t)(n + 1) * total] = Y1;
                     }
-                    if (NCK > 0 && (n + 2) % kTp2Ckpt == 0 && n + 2 < NMAT) {
+                    if (NCK > 0 && (n + 2) % ck == 0 && n + 2 < NMAT) {
                         // rates i <= n+2 are final from here on: only the others are saved
-                        const int c = (n + 2) / kTp2Ckpt - 1;
+                        const int c = (n + 2) / ck - 1;
 #pragma unroll
                         for (int i = 0; i < H; ++i)
                             if (base + i > n + 2) ckp[(c * NN + i) * PB] = X[i];
@@ -480,9 +475,9 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                     const int imin = n - 1 - base;           // lowest position with an active cell
                     if (imin < H)
                         tp2_rev_pair<H, PB, CH, P>(X, Pb, st, kc0 - (n + 1), vg0 + (base - n - 1) * PB, delta, imin);
-                    if (NCK > 0 && (n - 1) % kTp2Ckpt == 0 && n - 1 >= kTp2Ckpt) {
+                    if (NCK > 0 && (n - 1) % ck == 0 && n - 1 >= ck) {
                         // the reverse of steps >= n-1 leaves rates i <= n-1 untouched
-                        const int c = (n - 1) / kTp2Ckpt - 1;
+                        const int c = (n - 1) / ck - 1;
 #pragma unroll
                         for (int i = 0; i < H; ++i)
                             if (base + i > n - 1) X[i] = ckp[(c * NN + i) * PB];
@@ -563,9 +558,9 @@ bool f32_tp2_supports(int nn, int nmat) { return nn == 160 && nmat == 120; }
 
 int tp2_paths_per_block(int) { return Tp2Shape<160>::kBlock / 2; }
 
-size_t tp2_scratch_floats_per_block(int nn, int nmat)
+size_t tp2_scratch_floats_per_block(int nn, int nmat, int ckpt)
 {
-    return (size_t)(nmat + tp2_nckpt(nmat) * nn) * tp2_paths_per_block(nn);
+    return (size_t)(nmat + tp2_nckpt(nmat, ckpt) * nn) * tp2_paths_per_block(nn);
 }
 
 // Philox normals only in the fused kernel; the pair reads its normals from memory.

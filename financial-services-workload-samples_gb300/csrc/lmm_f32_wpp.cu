@@ -11,12 +11,13 @@
 // Reverse sweep without a stored trajectory: the forward saves, per step and
 // lane, Y_top = V + sqrt(delta) z at the lane's top rate (one float per lane
 // and step, in a per-warp device scratch that stays in L2), and the rates
-// every kWppReset steps. The reverse restarts each step from Y_top and runs
+// every ck steps (DevModel::ckpt, the engine's checkpoint interval; 0: none).
+// The reverse restarts each step from Y_top and runs
 // the Euler step backwards down the lane's own slots,
 //   L_{n,i} = L_{n+1,i} 2^-(a_k Y_i + c_k),  Y_{i-1} = Y_i - delta^2 lambda_k t_i,
-// so the serial chain is S cells long, not NN; at every kWppReset-th step it
+// so the serial chain is S cells long, not NN; at every ck-th step it
 // replaces the rebuilt rates by the saved ones, so FP32 rounding of the
-// reconstruction accumulates over at most kWppReset steps. The adjoint in log form
+// reconstruction accumulates over at most ck steps. The adjoint in log form
 // (Pb = L dV/dL) is
 //   S'_i = delta^2 sum_{j>=i} lambda_k Pb_j,  Pb_i += lambda_k t r S'_i
 //   dV/dlambda_k += Pb_i (Y_i - delta lambda_k) + t S'_i.
@@ -37,10 +38,6 @@ constexpr int kWppWarps = kWppBlock / 32;
 #ifndef LMM_WPP_PAD
 #define LMM_WPP_PAD 1
 #endif
-#ifndef LMM_WPP_RESET
-#define LMM_WPP_RESET 8
-#endif
-constexpr int kWppReset = LMM_WPP_RESET;   // the reverse restores the exact rates every kWppReset steps
 
 // Resident blocks the register budget is sized for: 6 (shared memory allows
 // no more at NN=160); 5 for S=8, which spills at 6.
@@ -51,10 +48,10 @@ __host__ __device__ constexpr int wpp_min_blocks(int S) { return S >= 8 ? 5 : 6;
 #endif
 
 // Scratch per warp, in floats: Y_top per step and lane, then the rates at
-// every kWppReset-th step, [checkpoint][slot][lane].
-__host__ __device__ constexpr size_t wpp_scratch_floats(int nmat, int S)
+// every ck-th step (ck = DevModel::ckpt; 0: none), [checkpoint][slot][lane].
+__host__ __device__ constexpr size_t wpp_scratch_floats(int nmat, int S, int ck)
 {
-    return (size_t)32 * nmat + (size_t)32 * S * ((nmat + kWppReset - 1) / kWppReset);
+    return (size_t)32 * nmat + (ck > 0 ? (size_t)32 * S * ((nmat + ck - 1) / ck) : 0);
 }
 
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -232,7 +229,7 @@ struct ZChunk {
 // MODE: Fused (value + all Greeks), Forward (value only) or Backward (Greeks
 // of vbar[scen] x value; the forward is recomputed from the same normals, so
 // no tape is needed). ytop: gridDim.x * kWppWarps blocks of
-// wpp_scratch_floats(nmat, S) floats of scratch, one per resident warp
+// wpp_scratch_floats(nmat, S, m.ckpt) floats of scratch, one per resident warp
 // (unused in Forward mode).
 template <int S, bool PHILOX, Mode MODE>
 __global__ void __launch_bounds__(kWppBlock, wpp_min_blocks(S))
@@ -252,8 +249,9 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     F2 *okk_s = reinterpret_cast<F2 *>(smem + Ly.okk);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned char *wbase = smem + Ly.warp0 + warp * Ly.per_warp;
-    float *yt = ytop + ((size_t)blockIdx.x * kWppWarps + warp) * wpp_scratch_floats(nmat, S) + lane;
-    float *ck = yt + (size_t)32 * nmat;     // ck[(c*S + s)*32]: rate of slot s at step c*kWppReset
+    const int ckn = m.ckpt;                 // the reverse restores the exact rates every ckn steps (0: never)
+    float *yt = ytop + ((size_t)blockIdx.x * kWppWarps + warp) * wpp_scratch_floats(nmat, S, ckn) + lane;
+    float *ck = yt + (size_t)32 * nmat;     // ck[(c*S + s)*32]: rate of slot s at step c*ckn
     float *vg_s = reinterpret_cast<float *>(wbase + Ly.vg);
     float *lw_s = reinterpret_cast<float *>(wbase + Ly.lw);
     float *bw_s = reinterpret_cast<float *>(wbase + Ly.bw);
@@ -308,9 +306,9 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             }
             // ---- forward ----
             for (int n = 0; n < nmat; ++n) {
-                if (MODE != Mode::Forward && n % kWppReset == 0) {
+                if (MODE != Mode::Forward && ckn > 0 && n % ckn == 0) {
 #pragma unroll
-                    for (int s = 0; s < S; ++s) ck[((n / kWppReset) * S + s) * 32] = L[s];
+                    for (int s = 0; s < S; ++s) ck[((n / ckn) * S + s) * 32] = L[s];
                 }
                 const float sqez = sqd * zc.get(n, zp, nmat, seed, gpath, lane);
                 const float y = wpp_fwd_step<S>(L, base, n, sqez, lane, kc_s, delta);
@@ -393,9 +391,9 @@ k_wpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 const float y = ynext;
                 if (n > 0) ynext = yt[(n - 1) * 32];
                 wpp_rev_step<S>(L, Pb, base, n, lane, y, kc_s, vg_s, delta);
-                if (n % kWppReset == 0) {
+                if (ckn > 0 && n % ckn == 0) {
 #pragma unroll
-                    for (int s = 0; s < S; ++s) L[s] = ck[((n / kWppReset) * S + s) * 32];
+                    for (int s = 0; s < S; ++s) L[s] = ck[((n / ckn) * S + s) * 32];
                 }
             }
             // ---- accumulate this path: value, deltas, vegas ----
@@ -493,7 +491,10 @@ int wpp_slots(int nn)
     return 0;
 }
 
-size_t wpp_scratch_floats_per_warp(int nn, int nmat) { return wpp_scratch_floats(nmat, wpp_slots(nn)); }
+size_t wpp_scratch_floats_per_warp(int nn, int nmat, int ckpt)
+{
+    return wpp_scratch_floats(nmat, wpp_slots(nn), ckpt);
+}
 
 bool f32_wpp_supports(int nn, int nmat)
 {

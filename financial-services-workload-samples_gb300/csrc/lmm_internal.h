@@ -30,6 +30,8 @@ struct DevModel {
     const double *optKd;                  // [nopt]
     const float *optWf;                   // [nopt] notional weights in that grouped order
     const double *optWd;                  // [nopt] (the reference's portfolio: all 1)
+    int ckpt;                             // steps between the rate checkpoints the
+                                          // FP32 reverse sweeps restore (0: none)
 };
 
 // Path partition of one launch: grid = nscen * items blocks; block b takes
@@ -46,6 +48,11 @@ struct Work {
 
 enum class Mode : int { Fused = 0, Forward = 1, Backward = 2 };
 
+// The calling thread's lmm_last_error() detail (lmm_capi.cpp): sets it and
+// returns `status`; the CUDA form maps the error to its LMM status.
+int record_error(int status, const char *what);
+int record_cuda_error(cudaError_t e, const char *what);
+
 // FP32 thread-per-path kernels (lmm_f32_tpp.cu, NN=80, NMAT=40).
 bool f32_tpp_supports(int nn, int nmat);
 int tpp_block_threads(Mode mode);     // threads per block = paths per batch
@@ -59,20 +66,22 @@ cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_
 bool f32_tp2_supports(int nn, int nmat);
 int tp2_paths_per_block(int nn);
 // Scratch of the fused kernel per block (floats): the lower half's drift sums
-// at the half boundary per step, and both halves' rate checkpoints.
-size_t tp2_scratch_floats_per_block(int nn, int nmat);
+// at the half boundary per step, and both halves' rate checkpoints, one every
+// ckpt steps (ckpt even; 0: none).
+size_t tp2_scratch_floats_per_block(int nn, int nmat, int ckpt);
 cudaError_t tp2_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks);
 cudaError_t launch_tp2_any(const DevModel &m, Mode mode, const float *z, uint64_t seed, int64_t path0,
                            bool philox, const Work &w, float *tape, const double *vbar, cudaStream_t s);
 // FP32 warp-per-path kernels (lmm_f32_wpp.cu, any NN <= kMaxNN; the reverse
 // sweep rebuilds each step from the forward's per-lane drift sums and takes
-// the saved rates every 8 steps).
+// the saved rates every DevModel::ckpt steps).
 bool f32_wpp_supports(int nn, int nmat);
 int wpp_block_threads();
 cudaError_t wpp_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks);
 // Device scratch the warp-per-path kernels take per warp (floats): the
-// forward's per-step drift sums at each lane's top rate, and rate checkpoints.
-size_t wpp_scratch_floats_per_warp(int nn, int nmat);
+// forward's per-step drift sums at each lane's top rate, and rate checkpoints
+// every ckpt steps (0: none).
+size_t wpp_scratch_floats_per_warp(int nn, int nmat, int ckpt);
 int wpp_slots(int nn);
 cudaError_t launch_wpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
                            int64_t path0, bool philox, const Work &w, float *tape,

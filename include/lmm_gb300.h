@@ -104,6 +104,23 @@ int lmm_engine_destroy(lmm_engine *e);
  * memsets on the stream and allocates nothing, so it can be recorded by a
  * stream capture and replayed. */
 int lmm_engine_set_stream(lmm_engine *e, void *stream);
+/* Checkpoint interval of the FP32 reverse sweep (fused calls). Storing the
+ * whole NN x NMAT trajectory per path, as the reference does (params.h:29
+ * L2_SIZE, liborSwaptionGreeks.cpp:76), would not fit on chip, so the
+ * reverse sweep runs each Euler step backwards from the drift sums the
+ * forward saved; the long-tenor kernels also save the rates every `steps`
+ * steps and restore them in the reverse, so that FP32 rounding of the
+ * backward steps accumulates over at most `steps` steps. 0: no rate
+ * checkpoints. The default is 8 for every shape but nn = 80, nmat = 40,
+ * whose kernel keeps all its drift sums on chip and takes no rate
+ * checkpoints (only 0 is accepted there: LMM_ERR_UNSUPPORTED otherwise).
+ * nn = 160, nmat = 120 runs its steps in pairs and needs an even interval
+ * (LMM_ERR_UNSUPPORTED otherwise); steps outside [0, nmat] is
+ * LMM_ERR_INVALID_ARG. Applies to later calls; a smaller interval may grow
+ * the engine's device scratch on the next call. */
+int lmm_engine_set_checkpoint_interval(lmm_engine *e, int32_t steps);
+/* The current interval (-1 for a NULL engine). */
+int32_t lmm_engine_checkpoint_interval(const lmm_engine *e);
 /* Blocks until all work enqueued on the engine's stream is done. */
 int lmm_engine_synchronize(lmm_engine *e);
 /* Launches enqueued by the last compute call (kernels only). */
