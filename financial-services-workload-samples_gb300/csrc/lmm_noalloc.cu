@@ -14,10 +14,17 @@
 // that name is a host-side stand-in, not a device address. The first call on
 // each device (with that device current) looks the address up with
 // cudaGetSymbolAddress, queries the kernel's occupancy and caches both; make
-// that first call before any stream capture.
+// that first call before any stream capture. The cache is keyed by the
+// device's context: after cudaDeviceReset the next call looks the address up
+// again in the new context (the array moves with the reloaded module).
+//
+// The model constants reach the scratch through a copy kernel that takes them
+// by value as its parameter: the launch carries its own copy of them, so no
+// host buffer has to outlive the call and the call never waits for the GPU.
 #include "lmm_gb300.h"
 #include "lmm_internal.h"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -53,8 +60,22 @@ static_assert(kMaxItems >= 64 * LMM_NOALLOC_MAX_SCEN, "scratch too small");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
+static_assert(sizeof(NoallocModel) % 4 == 0, "the model is copied in 32-bit words");
+static_assert(sizeof(NoallocModel) + 2 * sizeof(void *) <= 32000, "the model travels as a kernel parameter");
+
+// Copies the model (a kernel parameter, so the launch owns its own copy of
+// it) into the scratch and clears the non-finite flag.
+__global__ void k_noalloc_upload(const __grid_constant__ NoallocModel hm, NoallocModel *dst, int *flag)
+{
+    const unsigned *src = reinterpret_cast<const unsigned *>(&hm);
+    unsigned *d = reinterpret_cast<unsigned *>(dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(NoallocModel) / 4); i += blockDim.x) d[i] = src[i];
+    if (threadIdx.x == 0) *flag = 0;
+}
+
 struct DeviceSetup {
     bool ready = false;
+    unsigned long long ctx_id = 0;      // context the address belongs to
     unsigned char *scratch = nullptr;   // device address of g_noalloc_scratch
     int sms = 0, bps = 0;
 };
@@ -62,17 +83,59 @@ struct DeviceSetup {
 std::mutex g_mu;
 DeviceSetup g_setup[kMaxDevices];
 
+// The current context's unique id (cuCtxGetId through the runtime's driver
+// entry points, so the library needs no link against libcuda). *found is
+// false while the calling thread has no current context yet.
+int current_context_id(unsigned long long *id, bool *found)
+{
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess)
+            return lmm::record_error(LMM_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId unavailable");
+        get_current = reinterpret_cast<GetCurrent>(f1);
+        get_id = reinterpret_cast<GetId>(f2);
+    }
+    CUcontext ctx = nullptr;
+    *found = false;
+    if (get_current(&ctx) != CUDA_SUCCESS) return lmm::record_error(LMM_ERR_CUDA, "cuCtxGetCurrent failed");
+    if (!ctx) return LMM_OK;
+    if (get_id(ctx, id) != CUDA_SUCCESS) return lmm::record_error(LMM_ERR_CUDA, "cuCtxGetId failed");
+    *found = true;
+    return LMM_OK;
+}
+
 int setup_device(int dev, DeviceSetup *out)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     DeviceSetup &s = g_setup[dev];
-    if (!s.ready) {
+    unsigned long long ctx = 0;
+    bool found = false;
+    int rc = current_context_id(&ctx, &found);
+    if (rc != LMM_OK) return rc;
+    if (!s.ready || !found || s.ctx_id != ctx) {
+        s.ready = false;
         void *ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return LMM_ERR_CUDA;
+        // The lookup also makes the device's primary context current.
+        cudaError_t ce = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (ce != cudaSuccess) return lmm::record_cuda_error(ce, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        if (!ptr) return lmm::record_error(LMM_ERR_CUDA, "cudaGetSymbolAddress returned NULL");
+        if ((rc = current_context_id(&ctx, &found)) != LMM_OK) return rc;
+        if (!found) return lmm::record_error(LMM_ERR_CUDA, "no current CUDA context after the lookup");
         int sms = 0, bps = 0;
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return LMM_ERR_CUDA;
-        if (lmm::tpp_blocks_per_sm(lmm::Mode::Fused, false, &bps) != cudaSuccess || bps < 1) return LMM_ERR_CUDA;
+        ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (ce != cudaSuccess) return lmm::record_cuda_error(ce, "cudaDeviceGetAttribute");
+        ce = lmm::tpp_blocks_per_sm(lmm::Mode::Fused, false, &bps);
+        if (ce != cudaSuccess) return lmm::record_cuda_error(ce, "occupancy query");
+        if (bps < 1) return lmm::record_error(LMM_ERR_UNSUPPORTED, "the fused kernel does not fit on this device");
         s.scratch = static_cast<unsigned char *>(ptr);
+        s.ctx_id = ctx;
         s.sms = sms;
         s.bps = bps;
         s.ready = true;
@@ -88,14 +151,17 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
 {
     int rc = lmm_validate_params(p);
     if (rc != LMM_OK) return rc;
-    if (p->nn != kNN || p->nmat != kNMAT) return LMM_ERR_UNSUPPORTED;
-    if (p->nscen > LMM_NOALLOC_MAX_SCEN) return LMM_ERR_TOO_LARGE;
-    if (!d_z || !d_out || paths < 1) return LMM_ERR_INVALID_ARG;
-    if (paths > (int64_t(1) << 40)) return LMM_ERR_TOO_LARGE;
+    if (p->nn != kNN || p->nmat != kNMAT)
+        return lmm::record_error(LMM_ERR_UNSUPPORTED, "the no-allocation call covers nn=80, nmat=40 only");
+    if (p->nscen > LMM_NOALLOC_MAX_SCEN)
+        return lmm::record_error(LMM_ERR_TOO_LARGE, "nscen above LMM_NOALLOC_MAX_SCEN");
+    if (!d_z || !d_out) return lmm::record_error(LMM_ERR_INVALID_ARG, "NULL device pointer");
+    if (paths < 1) return lmm::record_error(LMM_ERR_INVALID_ARG, "paths must be >= 1");
+    if (paths > (int64_t(1) << 40)) return lmm::record_error(LMM_ERR_TOO_LARGE, "paths must be <= 2^40");
 
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return LMM_ERR_NO_DEVICE;
-    if (dev < 0 || dev >= kMaxDevices) return LMM_ERR_UNSUPPORTED;
+    if (cudaGetDevice(&dev) != cudaSuccess) return lmm::record_error(LMM_ERR_NO_DEVICE, "no CUDA device");
+    if (dev < 0 || dev >= kMaxDevices) return lmm::record_error(LMM_ERR_UNSUPPORTED, "device ordinal above 63");
     DeviceSetup ds;
     if ((rc = setup_device(dev, &ds)) != LMM_OK) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -128,11 +194,22 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
         hm.owd[slot] = 1.0;
     }
 
+    // About two waves of the device, capped by the partial-sum space.
+    const int64_t block = lmm::tpp_block_threads(lmm::Mode::Fused);
+    const int64_t nscen = p->nscen;
+    int64_t items = (2 * (int64_t)ds.sms * ds.bps + nscen - 1) / nscen;
+    if (items * nscen > kMaxItems) items = kMaxItems / nscen;
+    if (items < 1) items = 1;
+    int64_t ppt = (paths + block * items - 1) / (block * items);
+    items = (paths + block * ppt - 1) / (block * ppt);
+    if (ppt > 0x7fffffff) return lmm::record_error(LMM_ERR_TOO_LARGE, "too many paths per thread");
     unsigned char *base = ds.scratch;
-    if (cudaMemcpyAsync(base, &hm, sizeof(hm), cudaMemcpyHostToDevice, st) != cudaSuccess) return LMM_ERR_CUDA;
-    const NoallocModel *dmod = reinterpret_cast<const NoallocModel *>(base);
+    NoallocModel *dmod = reinterpret_cast<NoallocModel *>(base);
     int *flag = reinterpret_cast<int *>(base + kModelBytes);
     double *partial = reinterpret_cast<double *>(base + kModelBytes + kFlagBytes);
+    k_noalloc_upload<<<1, 256, 0, st>>>(hm, dmod, flag);
+    cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess) return lmm::record_cuda_error(ce, "model upload launch");
 
     lmm::DevModel m{};
     m.nn = kNN;
@@ -155,15 +232,6 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
     m.optWf = dmod->owf;
     m.optWd = dmod->owd;
 
-    // About two waves of the device, capped by the partial-sum space.
-    const int64_t block = lmm::tpp_block_threads(lmm::Mode::Fused);
-    const int64_t nscen = p->nscen;
-    int64_t items = (2 * (int64_t)ds.sms * ds.bps + nscen - 1) / nscen;
-    if (items * nscen > kMaxItems) items = kMaxItems / nscen;
-    if (items < 1) items = 1;
-    int64_t ppt = (paths + block * items - 1) / (block * items);
-    items = (paths + block * ppt - 1) / (block * ppt);
-    if (ppt > 0x7fffffff) return LMM_ERR_TOO_LARGE;
     lmm::Work w{};
     w.paths = paths;
     w.items = (int)items;
@@ -171,10 +239,9 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
     w.partial = partial;
     w.nout = kNout;
 
-    if (cudaMemsetAsync(flag, 0, sizeof(int), st) != cudaSuccess) return LMM_ERR_CUDA;
-    if (lmm::launch_tpp_any(m, lmm::Mode::Fused, d_z, 0, 0, false, w, nullptr, nullptr, st) != cudaSuccess)
-        return LMM_ERR_CUDA;
-    if (lmm::launch_finalize(partial, p->nscen, w.items, kNout, paths, d_out, d_se, flag, st) != cudaSuccess)
-        return LMM_ERR_CUDA;
+    ce = lmm::launch_tpp_any(m, lmm::Mode::Fused, d_z, 0, 0, false, w, nullptr, nullptr, st);
+    if (ce != cudaSuccess) return lmm::record_cuda_error(ce, "FP32 LMM kernel launch");
+    ce = lmm::launch_finalize(partial, p->nscen, w.items, kNout, paths, d_out, d_se, flag, st);
+    if (ce != cudaSuccess) return lmm::record_cuda_error(ce, "finalize launch");
     return LMM_OK;
 }

@@ -256,16 +256,17 @@ int lmm_mrg32k3a_normals_f32_device(uint32_t seed, int64_t first, int64_t count,
  * the library holds until the process exits.
  *   - Limits: nn = 80, nmat = 40 (LMM_ERR_UNSUPPORTED otherwise),
  *     nscen <= LMM_NOALLOC_MAX_SCEN and paths <= 2^40 (LMM_ERR_TOO_LARGE).
- *   - Works on the current device and enqueues on `stream`. The model
- *     constants are copied from host memory on the way in, so the call
- *     returns only after earlier work on `stream` has drained.
+ *   - Works on the current device and enqueues on `stream` without waiting:
+ *     the model constants travel as a kernel parameter, so nothing of the
+ *     caller's host memory is read after the call returns.
  *   - The first call on a device looks up the array's device address and the
  *     kernel's occupancy and caches them: make it before any stream capture.
+ *     After cudaDeviceReset the next call on that device looks them up again.
  *   - Every call shares the one array, which keeps the last call's
  *     contents: calls that overlap on the GPU (other streams, other host
  *     threads) race on it and must be serialised by the caller.
  *   - Non-finite results are not reported (there is no engine to hold the
- *     flag); check d_out. lmm_last_error() is not updated. */
+ *     flag); check d_out. Failures set lmm_last_error() as every call does. */
 #define LMM_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define LMM_NOALLOC_MAX_SCEN 8
 int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d_z, int64_t paths,

@@ -50,11 +50,18 @@ def test_noalloc_matches_engine_on_two_calls_in_a_row(nscen):
     r = ref.cpu().numpy().reshape(nscen, cfg.nout)
     r_se = ref_se.cpu().numpy().reshape(nscen, cfg.nout)
     stream = torch.cuda.current_stream().cuda_stream
+    outs = [torch.full((nscen * cfg.nout,), np.nan, dtype=torch.float64, device="cuda") for _ in range(4)]
     for call in range(2):
-        out = torch.full((nscen * cfg.nout,), np.nan, dtype=torch.float64, device="cuda")
-        se = torch.full_like(out, np.nan)
+        out, se = outs[2 * call], outs[2 * call + 1]
+        torch.cuda.synchronize()
+        free0, allocated0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
         assert _call(P, cfg, dz, n, out, se, stream) == 0
         torch.cuda.synchronize()
+        if call == 1:
+            # the first call may load the library's kernels; the second
+            # allocates no device memory at all
+            assert torch.cuda.mem_get_info()[0] == free0
+            assert torch.cuda.memory_allocated() == allocated0
         g = out.cpu().numpy().reshape(nscen, cfg.nout)
         g_se = se.cpu().numpy().reshape(nscen, cfg.nout)
         for s in range(nscen):
@@ -75,3 +82,4 @@ def test_noalloc_limits_are_errors():
     assert _call(P, many, dz, 64, out, se, 0) == -6
     one = cfgs().workload(1, 64)
     assert _call(P, one, dz, 0, out, se, 0) == -1
+    assert "paths" in P.last_error()
