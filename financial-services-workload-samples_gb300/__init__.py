@@ -31,7 +31,8 @@ EXPORTS = (
     "lmm_greeks_f32_host", "lmm_greeks_f32_device", "lmm_greeks_philox_host", "lmm_greeks_philox_device",
     "lmm_tape_create", "lmm_tape_destroy", "lmm_forward_f32_device", "lmm_backward_f32_device",
     "lmm_greeks_f64_host", "lmm_greeks_f64_device", "lmm_bump_greeks_f64_device",
-    "lmm_bump_greeks_f64_host", "lmm_normals_f32_device", "lmm_normals_f64_device",
+    "lmm_bump_greeks_f64_host", "lmm_bump_greeks_central_f64_device", "lmm_bump_greeks_central_f64_host",
+    "lmm_greeks_f32_rounding_device", "lmm_normals_f32_device", "lmm_normals_f64_device",
     "lmm_swaption_greeks", "lmm_swaption_greeks_f32", "lmm_greeks_f32_device_noalloc",
     "lmm_mrg32k3a_uniforms_device", "lmm_mrg32k3a_normals_f64_device", "lmm_mrg32k3a_normals_f32_device",
     "lmm_swaption_greeks_mrg32k3a", "lmm_swaption_greeks_mrg32k3a_f32",
@@ -101,6 +102,9 @@ def lib():
         "lmm_greeks_f64_device": ([vp, vp, i64, vp, vp], C.c_int),
         "lmm_bump_greeks_f64_device": ([vp, vp, i64, C.c_double, vp, vp], C.c_int),
         "lmm_bump_greeks_f64_host": ([vp, dp, i64, C.c_double, dp, dp], C.c_int),
+        "lmm_bump_greeks_central_f64_device": ([vp, vp, i64, C.c_double, vp, vp], C.c_int),
+        "lmm_bump_greeks_central_f64_host": ([vp, dp, i64, C.c_double, dp, dp], C.c_int),
+        "lmm_greeks_f32_rounding_device": ([vp, vp, i64, vp, vp, vp], C.c_int),
         "lmm_normals_f32_device": ([u64, i64, i64, i32, vp, vp], C.c_int),
         "lmm_normals_f64_device": ([u64, i64, i64, i32, C.c_double, C.c_double, vp, vp], C.c_int),
         "lmm_swaption_greeks": ([dp, C.c_int, C.c_double, C.c_double, C.c_int, dp, dp, C.c_int], C.c_int),
@@ -239,6 +243,11 @@ class Engine:
     def greeks_f32_device(self, d_z: int, paths: int, d_out: int, d_se: int = 0):
         _check(lib().lmm_greeks_f32_device(self.h, d_z, paths, d_out, d_se or None), "lmm_greeks_f32_device")
 
+    def greeks_f32_rounding_device(self, d_z: int, paths: int, d_out: int, d_se: int, d_err: int):
+        """FP32 results plus |FP32 - FP64| per output on the identical normals."""
+        _check(lib().lmm_greeks_f32_rounding_device(self.h, d_z, paths, d_out, d_se or None, d_err),
+               "lmm_greeks_f32_rounding_device")
+
     def greeks_philox(self, seed: int, paths: int, path0: int = 0):
         out, se = self._outs(self.nout)
         _check(lib().lmm_greeks_philox_host(self.h, seed, path0, paths, _dp(out), _dp(se)),
@@ -259,17 +268,19 @@ class Engine:
     def greeks_f64_device(self, d_z: int, paths: int, d_out: int, d_se: int = 0):
         _check(lib().lmm_greeks_f64_device(self.h, d_z, paths, d_out, d_se or None), "lmm_greeks_f64_device")
 
-    def bump_greeks_f64(self, z: np.ndarray, h: float, paths: int | None = None):
+    def bump_greeks_f64(self, z: np.ndarray, h: float, paths: int | None = None, central: bool = False):
+        """FP64 bump-and-revalue Greeks: one-sided, or central (+h and -h) differences."""
         z = np.ascontiguousarray(z, dtype=np.float64)
         paths = z.size // self.nmat if paths is None else paths
         out, se = self._outs(self.nout)
-        _check(lib().lmm_bump_greeks_f64_host(self.h, _dp(z), paths, h, _dp(out), _dp(se)),
-               "lmm_bump_greeks_f64_host")
+        fn = "lmm_bump_greeks_central_f64_host" if central else "lmm_bump_greeks_f64_host"
+        _check(getattr(lib(), fn)(self.h, _dp(z), paths, h, _dp(out), _dp(se)), fn)
         return out.reshape(self.nscen, self.nout), se.reshape(self.nscen, self.nout)
 
-    def bump_greeks_f64_device(self, d_z: int, paths: int, h: float, d_out: int, d_se: int = 0):
-        _check(lib().lmm_bump_greeks_f64_device(self.h, d_z, paths, h, d_out, d_se or None),
-               "lmm_bump_greeks_f64_device")
+    def bump_greeks_f64_device(self, d_z: int, paths: int, h: float, d_out: int, d_se: int = 0,
+                               central: bool = False):
+        fn = "lmm_bump_greeks_central_f64_device" if central else "lmm_bump_greeks_f64_device"
+        _check(getattr(lib(), fn)(self.h, d_z, paths, h, d_out, d_se or None), fn)
 
     # portfolio weights and per-swaption breakdown
     def set_weights(self, weights=None):

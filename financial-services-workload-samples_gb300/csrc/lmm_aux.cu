@@ -58,6 +58,35 @@ __global__ void k_bump_diff(double *mean, double *se, int nscen, int nout, doubl
     }
 }
 
+// Central differences from the 1+4nn variant means of one scenario
+// (base, +h on each of the 2nn inputs, -h on each): out[0] = base,
+// out[j] = (V(+h) - V(-h)) / 2h; se: the base's, 0 for the differences.
+__global__ void k_bump_central(const double *mean, const double *se_in, double *out, double *se,
+                               int nscen, int nn, double h)
+{
+    const int s = blockIdx.x;
+    const int nb = 1 + 4 * nn, nout = 1 + 2 * nn;
+    const double *m = mean + (size_t)s * nb;
+    for (int j = threadIdx.x; j < nout; j += blockDim.x) {
+        out[(size_t)s * nout + j] = j == 0 ? m[0] : (m[j] - m[2 * nn + j]) / (2.0 * h);
+        if (se) se[(size_t)s * nout + j] = j == 0 ? se_in[(size_t)s * nb] : 0.0;
+    }
+}
+
+// z64[i] = z32[i] (exact): the FP32 normals as FP64, for the FP64 kernel on
+// the identical inputs.
+__global__ void k_widen(const float *__restrict__ z32, double *__restrict__ z64, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        z64[i] = (double)z32[i];
+}
+
+// err[i] = |a[i] - b[i]|
+__global__ void k_abs_diff(const double *a, const double *b, double *err, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) err[i] = fabs(a[i] - b[i]);
+}
+
 __global__ void k_normals_f32(uint64_t seed, int64_t path0, int64_t paths, int nmat, float mean,
                               float sd, float *z)
 {
@@ -175,6 +204,25 @@ cudaError_t launch_finalize(const double *partial, int nscen, int items, int nou
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     dim3 block(kFinX, kFinY);
     k_finalize<<<(unsigned)blocks, block, 0, s>>>(partial, items, nout, paths, mean, se, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bump_central(const double *mean, const double *se_in, double *out, double *se, int nscen,
+                                int nn, double h, cudaStream_t s)
+{
+    k_bump_central<<<nscen, 256, 0, s>>>(mean, se_in, out, se, nscen, nn, h);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_widen(const float *z32, double *z64, int64_t n, cudaStream_t s)
+{
+    k_widen<<<grid_for(n, 256), 256, 0, s>>>(z32, z64, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_abs_diff(const double *a, const double *b, double *err, int n, cudaStream_t s)
+{
+    k_abs_diff<<<(n + 255) / 256, 256, 0, s>>>(a, b, err, n);
     return cudaGetLastError();
 }
 

@@ -113,6 +113,7 @@ struct lmm_engine {
     double *wd_rows = nullptr;
     DevBuf partial, z32, z64, out, se, flag, vbar;
     DevBuf wscratch;               // warp-per-path kernels: Y_top per warp, step and lane
+    DevBuf bumpvar;                // central bumps: the variants' means and standard errors
     std::map<int, int> bps;        // cached blocks per SM per kernel variant
     int32_t last_launches = 0;
     bool timing = false;
@@ -385,7 +386,7 @@ int run_f64(lmm_engine *e, const double *d_z, int64_t paths, double *d_mean, dou
     return LMM_OK;
 }
 
-int run_bump(lmm_engine *e, const double *d_z, int64_t paths, double h, double *d_mean,
+int run_bump(lmm_engine *e, const double *d_z, int64_t paths, double h, bool central, double *d_mean,
              double *d_se)
 {
     LMM_TRY(check_paths(paths));
@@ -394,17 +395,28 @@ int run_bump(lmm_engine *e, const double *d_z, int64_t paths, double h, double *
     LMM_TRY(set_device(e));
     int bps = 0;
     LMM_TRY(blocks_per_sm(e, 4, Mode::Fused, false, &bps));
-    const int nb = 1 + 2 * e->nn;
+    const int nb = central ? 1 + 4 * e->nn : 1 + 2 * e->nn;
     Work w{};
     LMM_TRY(plan(e, (int64_t)e->nscen * nb, paths, lmm::f64_block_threads(), bps, 1, &w));
     LMM_TRY(e->flag.ensure(sizeof(int)));
+    // central: the 1+4nn variant means (and their standard errors) go to the
+    // engine's scratch and are differenced into the caller's 1+2nn outputs
+    double *vmean = d_mean, *vse = d_se;
+    if (central) {
+        LMM_TRY(e->bumpvar.ensure(2 * sizeof(double) * (size_t)e->nscen * nb));
+        vmean = e->bumpvar.as<double>();
+        vse = vmean + (size_t)e->nscen * nb;
+    }
     LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
     mark(e, 0);
-    LMM_CK(lmm::launch_f64_bump(e->dm, d_z, h, w, e->stream));
+    LMM_CK(lmm::launch_f64_bump(e->dm, d_z, h, central, w, e->stream));
     mark(e, 1);
-    LMM_CK(lmm::launch_finalize(w.partial, e->nscen * nb, w.items, 1, paths, d_mean, d_se,
+    LMM_CK(lmm::launch_finalize(w.partial, e->nscen * nb, w.items, 1, paths, vmean, vse,
                                 e->flag.as<int>(), e->stream));
-    LMM_CK(lmm::launch_bump_diff(d_mean, d_se, e->nscen, nb, h, e->stream));
+    if (central)
+        LMM_CK(lmm::launch_bump_central(vmean, vse, d_mean, d_se, e->nscen, e->nn, h, e->stream));
+    else
+        LMM_CK(lmm::launch_bump_diff(d_mean, d_se, e->nscen, nb, h, e->stream));
     mark(e, 2);
     e->last_launches = 3;
     return LMM_OK;
@@ -1039,6 +1051,24 @@ int lmm_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, doubl
     return run_f64(e, d_z, paths, d_out, d_se);
 }
 
+int lmm_greeks_f32_rounding_device(lmm_engine *e, const float *d_z, int64_t paths, double *d_out, double *d_se,
+                                   double *d_err)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    if (!d_err) return fail(LMM_ERR_INVALID_ARG, "rounding-error pointer is NULL");
+    LMM_TRY(run_f32(e, Mode::Fused, d_z, 0, 0, false, paths, nullptr, nullptr, d_out, d_se));
+    const int32_t l32 = e->last_launches;
+    const size_t nz = (size_t)paths * e->nmat;
+    const int nout = 1 + 2 * e->nn;
+    LMM_TRY(e->z64.ensure(sizeof(double) * nz));
+    LMM_TRY(ensure_outputs(e, nout));
+    LMM_CK(lmm::launch_widen(d_z, e->z64.as<double>(), (int64_t)nz, e->stream));
+    LMM_TRY(run_f64(e, e->z64.as<double>(), paths, e->out.as<double>(), e->se.as<double>()));
+    LMM_CK(lmm::launch_abs_diff(d_out, e->out.as<double>(), d_err, e->nscen * nout, e->stream));
+    e->last_launches = l32 + e->last_launches + 2;
+    return LMM_OK;
+}
+
 int lmm_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double *out, double *se)
 {
     if (!e || !z || !out) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
@@ -1056,11 +1086,18 @@ int lmm_bump_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, 
                                double *d_out, double *d_se)
 {
     if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
-    return run_bump(e, d_z, paths, h, d_out, d_se);
+    return run_bump(e, d_z, paths, h, false, d_out, d_se);
 }
 
-int lmm_bump_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double h, double *out,
-                             double *se)
+int lmm_bump_greeks_central_f64_device(lmm_engine *e, const double *d_z, int64_t paths, double h,
+                                       double *d_out, double *d_se)
+{
+    if (!e) return fail(LMM_ERR_INVALID_ARG, "engine is NULL");
+    return run_bump(e, d_z, paths, h, true, d_out, d_se);
+}
+
+namespace {
+int bump_host(lmm_engine *e, const double *z, int64_t paths, double h, bool central, double *out, double *se)
 {
     if (!e || !z || !out) return fail(LMM_ERR_INVALID_ARG, "NULL argument");
     LMM_TRY(check_paths(paths));
@@ -1069,8 +1106,21 @@ int lmm_bump_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, doub
     LMM_TRY(e->z64.ensure(zb));
     LMM_TRY(ensure_outputs(e, 1 + 2 * e->nn));
     LMM_CK(cudaMemcpyAsync(e->z64.p, z, zb, cudaMemcpyHostToDevice, e->stream));
-    LMM_TRY(run_bump(e, e->z64.as<double>(), paths, h, e->out.as<double>(), e->se.as<double>()));
+    LMM_TRY(run_bump(e, e->z64.as<double>(), paths, h, central, e->out.as<double>(), e->se.as<double>()));
     return fetch(e, 1 + 2 * e->nn, out, se);
+}
+}  // namespace
+
+int lmm_bump_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double h, double *out,
+                             double *se)
+{
+    return bump_host(e, z, paths, h, false, out, se);
+}
+
+int lmm_bump_greeks_central_f64_host(lmm_engine *e, const double *z, int64_t paths, double h, double *out,
+                                     double *se)
+{
+    return bump_host(e, z, paths, h, true, out, se);
 }
 
 // ---- normals -------------------------------------------------------------------

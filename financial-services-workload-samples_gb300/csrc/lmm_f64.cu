@@ -170,9 +170,10 @@ k_f64_greeks(const DevModel m, const double *__restrict__ z, const Work w)
 
 // Plain FP64 bump-and-revalue: block b covers virtual scenario vs = b/items
 // = (scenario, variant j); j = 0 is the base, j = 1..nn bumps L0[j-1] by h,
-// j = nn+1..2nn bumps lambda[j-nn-1] by h. Output per variant: mean value.
+// j = nn+1..2nn bumps lambda[j-nn-1] by h; with `central`, j = 2nn+1..4nn
+// repeat those 2nn inputs bumped by -h. Output per variant: mean value.
 __global__ void __launch_bounds__(kF64Block)
-k_f64_bump(const DevModel m, const double *__restrict__ z, double h, const Work w)
+k_f64_bump(const DevModel m, const double *__restrict__ z, double h, int central, const Work w)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nn = m.nn, nmat = m.nmat, M = nn - nmat;
@@ -183,11 +184,14 @@ k_f64_bump(const DevModel m, const double *__restrict__ z, double h, const Work 
     double *acc_s = okw_s + kMaxNopt;
     int *ost_s = reinterpret_cast<int *>(acc_s + NW * 2);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nb = 1 + 2 * nn;
+    const int nb = central ? 1 + 4 * nn : 1 + 2 * nn;
     const int vs = blockIdx.x / w.items, item = blockIdx.x % w.items;
-    const int scen = vs / nb, var = vs % nb;
+    const int scen = vs / nb, vb = vs % nb;
+    // input bumped: 1..nn the rate L0[var-1], nn+1..2nn lambda[var-nn-1]; by hb
+    const int var = vb > 2 * nn ? vb - 2 * nn : vb;
+    const double hb = vb > 2 * nn ? -h : h;
     for (int i = tid; i < nn; i += kF64Block)
-        lam_s[i] = m.lamd[i] + ((var > nn && i == var - nn - 1) ? h : 0.0);
+        lam_s[i] = m.lamd[i] + ((var > nn && i == var - nn - 1) ? hb : 0.0);
     for (int i = tid; i <= M; i += kF64Block) ost_s[i] = m.opt_start[i];
     for (int i = tid; i < m.nopt; i += kF64Block) {
         okd_s[i] = m.optKd[i];
@@ -204,7 +208,7 @@ k_f64_bump(const DevModel m, const double *__restrict__ z, double h, const Work 
         const int64_t pl = ibase + (int64_t)j * kF64Block + tid;
         const bool active = pl < w.paths;
         const double *zp = z + (active ? pl : w.paths - 1) * nmat;
-        for (int i = 0; i < nn; ++i) L[i] = L0[i] + ((var >= 1 && var <= nn && i == var - 1) ? h : 0.0);
+        for (int i = 0; i < nn; ++i) L[i] = L0[i] + ((var >= 1 && var <= nn && i == var - 1) ? hb : 0.0);
         forward_f64(L, nullptr, zp, lam_s, nn, nmat, d, sqd);
         double disc;
         unsigned long long mask;
@@ -255,12 +259,12 @@ cudaError_t launch_f64_greeks(const DevModel &m, const double *z, const Work &w,
     return cudaGetLastError();
 }
 
-cudaError_t launch_f64_bump(const DevModel &m, const double *z, double h, const Work &w,
+cudaError_t launch_f64_bump(const DevModel &m, const double *z, double h, bool central, const Work &w,
                             cudaStream_t s)
 {
-    const int nb = 1 + 2 * m.nn;
+    const int nb = central ? 1 + 4 * m.nn : 1 + 2 * m.nn;
     const size_t sm = f64_smem_bytes(1);
-    k_f64_bump<<<(unsigned)((int64_t)m.nscen * nb * w.items), kF64Block, sm, s>>>(m, z, h, w);
+    k_f64_bump<<<(unsigned)((int64_t)m.nscen * nb * w.items), kF64Block, sm, s>>>(m, z, h, central ? 1 : 0, w);
     return cudaGetLastError();
 }
 

@@ -91,10 +91,11 @@ cudaError_t launch_wpp_any(const DevModel &m, Mode mode, const float *z, uint64_
 int f64_block_threads();
 cudaError_t f64_blocks_per_sm(bool bump, int *blocks);
 cudaError_t launch_f64_greeks(const DevModel &m, const double *z, const Work &w, cudaStream_t s);
-// Bumped forward re-runs: 1 + 2nn variants per scenario; the launch's
-// virtual scenarios are (scenario, variant) and each reduces one output, the
+// Bumped forward re-runs: 1 + 2nn variants per scenario (1 + 4nn with
+// `central`: each input bumped by +h and by -h); the launch's virtual
+// scenarios are (scenario, variant) and each reduces one output, the
 // variant's value (w.nout = 1).
-cudaError_t launch_f64_bump(const DevModel &m, const double *z, double h, const Work &w,
+cudaError_t launch_f64_bump(const DevModel &m, const double *z, double h, bool central, const Work &w,
                             cudaStream_t s);
 
 // Sums the per-item partials of each scenario in a fixed order and writes
@@ -105,6 +106,14 @@ cudaError_t launch_finalize(const double *partial, int nscen, int items, int nou
 // (out[j]-out[0])/h for j >= 1, per scenario.
 cudaError_t launch_bump_diff(double *mean, double *se, int nscen, int nout, double h,
                              cudaStream_t s);
+// Central differences (V(+h) - V(-h)) / 2h from the 1+4nn variant means per
+// scenario [nscen][1+4nn] into out/se [nscen][1+2nn].
+cudaError_t launch_bump_central(const double *mean, const double *se_in, double *out, double *se, int nscen,
+                                int nn, double h, cudaStream_t s);
+// z64 = (double)z32, element by element (n elements).
+cudaError_t launch_widen(const float *z32, double *z64, int64_t n, cudaStream_t s);
+// err = |a - b|, element by element (n elements).
+cudaError_t launch_abs_diff(const double *a, const double *b, double *err, int n, cudaStream_t s);
 
 // FFMA throughput probe: `blocks` x 256 threads, `iters` iterations of 16
 // independent FMA chains each; one float per thread to `sink`.

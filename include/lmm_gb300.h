@@ -187,6 +187,15 @@ int lmm_backward_f32_device(lmm_engine *e, const float *d_z, const lmm_tape *t,
 int lmm_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double *out, double *se);
 int lmm_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, double *d_out,
                           double *d_se);
+/* The FP32 results of lmm_greeks_f32_device (d_out, d_se) and, per output,
+ * their rounding error d_err = |FP32 result - FP64 result| on the identical
+ * normals (the FP64 kernel run on d_z widened to FP64), so that each
+ * result's arithmetic error is reported apart from its Monte Carlo standard
+ * error d_se. d_err has the layout of d_out. Costs one FP64 run and
+ * paths * nmat * 8 bytes of engine scratch. The reference reports its value
+ * and one delta (main.cpp:91-92) with neither. */
+int lmm_greeks_f32_rounding_device(lmm_engine *e, const float *d_z, int64_t paths, double *d_out,
+                                   double *d_se, double *d_err);
 /* FP64 forward only, re-run with bumped inputs: one-sided differences
  * (V(theta + h e_j) - V(theta)) / h for the nn L0[i] and the nn lambda[k];
  * out/se layout as above (se is the standard error of the value only; the
@@ -195,6 +204,17 @@ int lmm_bump_greeks_f64_device(lmm_engine *e, const double *d_z, int64_t paths, 
                                double *d_out, double *d_se);
 int lmm_bump_greeks_f64_host(lmm_engine *e, const double *z, int64_t paths, double h,
                              double *out, double *se);
+/* FP64 central differences under common random numbers:
+ * (V(theta + h e_j) - V(theta - h e_j)) / 2h for the nn L0[i] and the nn
+ * lambda[k], all 1 + 4nn forward runs on the same normals; out/se layout and
+ * se convention as lmm_bump_greeks_f64_*. This is the finite-difference
+ * check of the FP32 adjoint (bump 1e-6 in the headline workload); the
+ * reference's own sensitivities come from its adjoint
+ * (liborSwaptionGreeks.cpp:86-117), which this cross-checks. */
+int lmm_bump_greeks_central_f64_device(lmm_engine *e, const double *d_z, int64_t paths, double h,
+                                       double *d_out, double *d_se);
+int lmm_bump_greeks_central_f64_host(lmm_engine *e, const double *z, int64_t paths, double h,
+                                     double *out, double *se);
 
 /* ---- portfolio weights and per-swaption breakdown ----------------------- */
 /* The reference prices a fixed portfolio: every swaption with notional 100
