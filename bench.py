@@ -15,8 +15,8 @@ already in HBM, CUDA events on the launching stream); `e2e` is the same metric
 through the host C-ABI call lmm_greeks_f32_host with the normals in pinned host
 memory (host->device copy and result read-back inside the timed region).
 --impl reference times the reference's CPU algorithm for the same workload on
-the host cores (the C restatement under oracle/, since the reference tree is
-not available where this runs).
+the host cores (the C restatement under oracle/, built like the reference's
+own CPU build, since the reference tree is not available where this runs).
 """
 from __future__ import annotations
 
@@ -54,6 +54,12 @@ OPS_FWD_CELL = 11
 # reciprocal in the forward and again in the reverse reconstruction; the
 # payoff and its adjoint take 2*NN reciprocals.
 MUFU_PER_CELL = 4
+
+
+# Paths of the FP64 central-difference check in the accuracy section.
+CENTRAL_FD_PATHS = 16384
+# Wall-clock budget of the reference arm's warm-up and timed steps together.
+REF_BUDGET_S = 150.0
 
 
 def cells(nn, nmat):
@@ -147,35 +153,49 @@ class ClockSampler:
                 "power_w_max": max(power) if power else None, "reasons": sorted(reasons)}
 
 
-def cpu_baseline_port(cfg, target_s=3.0, threads=0):
+CPUBASE_NOTE = ("the oracle's C restatement of liborSwaptionGreeks.cpp:34-211 built like the reference's own "
+                "CPU build (LiborMarketModel/compile.sh: -O3, OpenMP over 16-path blocks, omp simd lanes, "
+                "fast floating-point model with vector math, explicit vector target)")
+
+
+def _time_work(O, cfg, z, n, threads, build):
+    t0 = time.perf_counter()
+    O.reference_work(cfg, z, n, threads, build=build)
+    return max(time.perf_counter() - t0, 1e-6)
+
+
+def cpu_baseline_port(cfg, target_s=10.0, threads=0):
     """The reference's per-path work (value + delta adjoint) on the host cores,
-    through the oracle's C restatement, on a bounded sample of the workload."""
+    through the oracle's C restatement built like the reference's own build,
+    on a bounded sample of the workload (about target_s seconds); beside it
+    the same on one core and the portable (checker) build on all cores."""
     from oracle import oracle as O
     threads = threads or O.max_threads()
-    calib = 2048
+    calib = 4096
     z = O.normals_f64(7, calib, cfg.nmat)
-    t0 = time.perf_counter()
-    O.reference_work(cfg, z, calib, threads)
-    dt = max(time.perf_counter() - t0, 1e-6)
-    n = int(min(4_194_304, max(calib, calib * target_s / dt)))
+    dt = _time_work(O, cfg, z, calib, threads, "tuned")
+    n = int(min(cfg.paths, max(calib, calib * target_s / dt)))
     n = max(16, n - n % 16)
     z = O.normals_f64(7, n, cfg.nmat)
-    t0 = time.perf_counter()
-    O.reference_work(cfg, z, n, threads)
-    dt = time.perf_counter() - t0
-    # the same on one core, on a sample sized for about a tenth of the time
+    dt = _time_work(O, cfg, z, n, threads, "tuned")
     n1 = max(16, int(n / max(threads, 1) / 10) // 16 * 16)
-    t1 = time.perf_counter()
-    O.reference_work(cfg, z, n1, 1)
-    dt1 = time.perf_counter() - t1
+    dt1 = _time_work(O, cfg, z, n1, 1, "tuned")
+    nc = max(16, n // 4 // 16 * 16)
+    dtc = _time_work(O, cfg, z, nc, threads, "checker")
     return {"value": n / dt, "unit": "paths/s", "cores": threads, "kind": "port",
-            "value_1core": n1 / dt1,
+            "value_1core": n1 / dt1, "value_portable_build": nc / dtc,
+            "build": "oracle/_build/liblmm_cpubase.so (" + " ".join(O.build_ref.CPUBASE_FLAGS[:5]) + " "
+                     + " ".join(O.build_ref._cpu_target_flags()) + ")",
             "sample": f"{n} paths of the same workload (FP64, value + {cfg.nn} deltas by the reference's "
-                      f"adjoint; the reference computes no vegas), {dt:.2f} s wall on {threads} threads",
+                      f"adjoint; the reference computes no vegas), {dt:.2f} s wall on {threads} threads; "
+                      f"value_portable_build: {nc} paths through the checker build (-O3, no fast math)",
             "seconds": dt}
 
 
 def run_reference_arm(args):
+    """The reference's CPU algorithm for the workload, on all host cores: per
+    step the workload's full path count when the whole run fits in about
+    REF_BUDGET_S seconds, else the largest multiple of 16 paths that does."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -183,24 +203,33 @@ def run_reference_arm(args):
     cfg = cfgm.workload(WORKLOAD)
     from oracle import oracle as O
     threads = O.max_threads()
-    sample = 65536
+    calib = 65536
+    zc = O.normals_f64(11, calib, cfg.nmat)
+    _time_work(O, cfg, zc, calib, threads, "tuned")
+    per_path = _time_work(O, cfg, zc, calib, threads, "tuned") / calib
+    del zc
+    fit = int(REF_BUDGET_S / max(per_path, 1e-12) / (args.steps + args.warmup))
+    sample = max(16, min(cfg.paths, fit) // 16 * 16)
     z = O.normals_f64(11, sample, cfg.nmat)
     for _ in range(args.warmup):
-        O.reference_work(cfg, z, sample, threads)
+        O.reference_work(cfg, z, sample, threads, build="tuned")
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        O.reference_work(cfg, z, sample, threads)
+        O.reference_work(cfg, z, sample, threads, build="tuned")
     dt = time.perf_counter() - t0
     v = args.steps * sample / dt
+    why = ("the workload's full path count" if sample == cfg.paths else
+           f"{sample} of the workload's {cfg.paths} paths per step, so that {args.warmup}+{args.steps} "
+           f"steps fit in about {REF_BUDGET_S:.0f} s")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "paths/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: Philox4x32-10 + Box-Muller FP64 normals",
             "config": {"workload": cfg.name, "nn": cfg.nn, "nmat": cfg.nmat, "paths_per_step": sample,
+                       "paths_per_step_why": why,
                        "work": f"value + {cfg.nn} deltas per path (the reference's adjoint; no vegas)"},
             "cpu_baseline": {"value": v, "unit": "paths/s", "cores": threads, "kind": "port",
-                             "sample": f"{sample} paths per step, FP64, C restatement of "
-                                       "liborSwaptionGreeks.cpp:34-211 with OpenMP over 16-path blocks"},
+                             "sample": f"{sample} paths per step, FP64, " + CPUBASE_NOTE},
             "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -295,7 +324,29 @@ def run_ours(args):
         acc = {"reference": "FP64 GPU kernel (pinned to the FP64 CPU oracle at 1e-12) on the identical normals",
                "max_rel_err_value": err[0], "max_rel_err_deltas": err[1], "max_rel_err_vegas": err[2],
                "tolerance": 1e-4, "rule": "|f32-f64| / max(|f64|, 1% of the largest of its group)",
-               "max_abs_err_over_mc_se": float(np.max(np.abs(res32 - r64) / np.maximum(se32, 1e-300)))}
+               "max_abs_err_over_mc_se": float(np.max(np.abs(res32 - r64) / np.maximum(se32, 1e-300))),
+               # per output, in output order (value, dV/dL0[0..NN-1], dV/dlambda[0..NN-1]): the
+               # FP32 result's rounding error |FP32 - FP64| beside its Monte Carlo standard error
+               "rounding_error": [float(f"{x:.3g}") for x in np.abs(res32 - r64)],
+               "se": [float(f"{x:.3g}") for x in se32]}
+        # FP64 central differences (h = 1e-6, common random numbers) on the
+        # first CENTRAL_FD_PATHS paths, against the FP32 adjoint on those paths
+        nf = min(n, CENTRAL_FD_PATHS)
+        dzf = dz[: nf * nmat]
+        dzf64 = dzf.double()
+        fd = torch.zeros(nout, dtype=torch.float64, device=dev)
+        a32 = torch.zeros(nout, dtype=torch.float64, device=dev)
+        eng.bump_greeks_f64_device(dzf64.data_ptr(), nf, 1e-6, fd.data_ptr(), central=True)
+        eng.greeks_f32_device(dzf.data_ptr(), nf, a32.data_ptr())
+        eng.synchronize()
+        fd, a32 = fd.cpu().numpy(), a32.cpu().numpy()
+        del dzf64
+        errf = []
+        for sl in (slice(1, 1 + cfg.nn), slice(1 + cfg.nn, nout)):
+            den = np.maximum(np.abs(fd[sl]), 1e-2 * np.abs(fd[sl]).max())
+            errf.append(float(np.max(np.abs(a32[sl] - fd[sl]) / np.where(den > 0, den, 1.0))))
+        acc["central_fd"] = {"paths": nf, "h": 1e-6, "max_rel_err_deltas": errf[0], "max_rel_err_vegas": errf[1],
+                             "method": "FP64 (V(+h) - V(-h)) / 2h, 1+4NN forward runs on the identical normals"}
 
     # ---- phase split: forward (+payoff, tape write) and backward (tape read,
     # payoff adjoint, reverse sweep) as separate calls of the C-ABI pair --------
@@ -503,7 +554,7 @@ def main():
     ap.add_argument("--paths", type=int, default=None,
                     help="paths per step (default: the workload's 4,194,304); smaller only for profiling")
     ap.add_argument("--bump-paths", type=int, default=16384)
-    ap.add_argument("--cpu-seconds", type=float, default=3.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--kernel-times", action="store_true",
                     help="read the main-kernel time after every timed step (adds a host sync per step)")
     ap.add_argument("--skip-accuracy", action="store_true")
