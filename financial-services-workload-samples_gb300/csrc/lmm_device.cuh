@@ -7,6 +7,12 @@
 
 #include "lmm_internal.h"
 
+// 1: the FP32 kernels' 32-path column sums are TwoSum-compensated before
+// they reach their FP64 accumulators (two_sum_acc); 0: plain FP32 sums.
+#ifndef LMM_COMP_SUMS
+#define LMM_COMP_SUMS 1
+#endif
+
 namespace lmm {
 
 // MUFU approximations issued directly (PTX ISA: rcp.approx.ftz.f32,
@@ -143,6 +149,18 @@ __device__ __forceinline__ F2 f2_add(F2 x, F2 y)
 }
 
 __device__ __forceinline__ F2 f2_add(F2 x, float y) { return f2_add(x, F2{y, 0.0f}); }
+
+// Compensated FP32 summation: s + c carries the running sum, s its rounded
+// value and c the accumulated rounding errors of the additions, each
+// recovered exactly by TwoSum (Knuth, TAOCP vol. 2, 4.2.2). The result is
+// about as accurate as an FP64 sum of the same FP32 terms.
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x)
+{
+    const float t = __fadd_rn(s, x);
+    const float v = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(x, v)));
+    s = t;
+}
 
 // The F2 nearest a double (host data staged once per block).
 __device__ __forceinline__ F2 f2_from(double x)

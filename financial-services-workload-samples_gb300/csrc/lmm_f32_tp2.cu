@@ -199,20 +199,24 @@ __device__ __forceinline__ void tp2_rev_pair(float (&X)[H], float (&Pb)[H], floa
 
 // Column sums over a pair's 32 paths of H rows (stride PB): lane handles rows
 // lane, lane+32, ...; the (t+lane)&31 rotation keeps the lanes on distinct
-// banks. Adds sums and sums of squares into FP64 accumulators.
+// banks. Adds sums (TwoSum-compensated, LMM_COMP_SUMS) and sums of squares
+// into FP64 accumulators.
 template <int H, int PB>
 __device__ __forceinline__ void tp2_rows_reduce(const float *rows, int lane, double *acc, int nout, int off)
 {
     for (int k = lane; k < H; k += 32) {
         const float *col = rows + k * PB;
-        float a = 0.0f, a2 = 0.0f;
+        float a = 0.0f, c = 0.0f, a2 = 0.0f;
 #pragma unroll 8
         for (int t = 0; t < 32; ++t) {
             const float x = col[(t + lane) & 31];
-            a += x;
+            if (LMM_COMP_SUMS)
+                two_sum_acc(a, c, x);
+            else
+                a += x;
             a2 = fmaf(x, x, a2);
         }
-        acc[off + k] += (double)a;
+        acc[off + k] += (double)a + (double)c;
         acc[nout + off + k] += (double)a2;
     }
 }

@@ -31,7 +31,8 @@
 //   dV/dlambda_k += Pb_i (V_i + sqez - delta lambda_k) + delta^2 t S.
 // The kernel carries S' = delta^2 S (S' += delta^2 lambda_k Pb_i, Pb_i +=
 // lambda_k r t S'), which saves a multiply per cell. Vega slots of no-op cells
-// (k < 0) are NMAT spare rows per thread that are never read.
+// (k < 0) are spare rows in front of row 0 that are never read; a reverse
+// window touches rows k >= 1 - (its chunk of positions), so four suffice.
 // The reconstruction is a serial chain (exp -> rcp -> drift sum) per step, so
 // steps are processed as a skewed wavefront: cell (n,i) next to cell
 // (n-1,i+1), next to (n-2,i+2), ..., G independent chains in one instruction
@@ -47,6 +48,8 @@
 // accumulators; each block writes FP64 partial sums that lmm_aux.cu adds in a
 // fixed order, so results are bit-reproducible.
 #include "lmm_device.cuh"
+
+#include <cuda_bf16.h>
 
 // Threads per block of the fused kernel: 254 registers per thread leave room
 // for 8 warps per SM, run as one block of 256 threads so that the block
@@ -115,6 +118,16 @@
 #ifndef LMM_TPP_YRUN
 #define LMM_TPP_YRUN 1
 #endif
+// 1: Kahan-compensated per-thread vega rows (the compensations held as BF16
+// rows beside the FP32 rows); 0: plain FP32 read-modify-writes.
+#ifndef LMM_TPP_VCOMP
+#define LMM_TPP_VCOMP 0
+#endif
+// Forward steps run together as a skewed wavefront in the fused kernel: 2
+// (pairs, fwd_pair_window) or 4 (fwd_group_window).
+#ifndef LMM_TPP_FGROUP
+#define LMM_TPP_FGROUP 2
+#endif
 // Positions ahead at which the step windows load the constants of a rate
 // from shared memory (0: at the position that first uses them), with the
 // normals read from memory and with Philox normals (more live registers).
@@ -153,6 +166,9 @@ struct TppLayout {
     static constexpr int NW = B / 32;
     static constexpr int M = NN - NMAT;
     static constexpr int PAD = NMAT;                 // k = i-n-1 >= -NMAT
+    // Spare vega rows in front of row 0: a reverse window flushes rows
+    // k >= 1 - (its chunk of positions) >= -3.
+    static constexpr int VPAD = 4;
     static constexpr int NOUT = MODE == Mode::Fused ? 1 + 2 * NN : (MODE == Mode::Forward ? 1 : 2 * NN);
     static constexpr int kc = 0;                                     // float4[PAD+NN]
     static constexpr int il0 = align16(kc + 16 * (PAD + NN));        // float[NN]
@@ -162,11 +178,14 @@ struct TppLayout {
     static constexpr int okk = align16(owf + 4 * kMaxNopt);          // F2[kMaxNopt]: K delta
     static constexpr int vt = align16(okk + 8 * kMaxNopt);           // float[NMAT][B]
     static constexpr int vt_bytes = MODE == Mode::Fused ? 4 * NMAT * B : 0;
-    static constexpr int vg = vt + vt_bytes;                         // float[PAD+NN][B]
-    // Backward/Fused: per-thread vega rows k = -PAD..NN-1; the payoff also
+    static constexpr int vg = vt + vt_bytes;                         // float[VPAD+NN][B]
+    // Backward/Fused: per-thread vega rows k = -VPAD..NN-1; the payoff also
     // stages the annuity rates there. Forward: only the M staging rows.
-    static constexpr int vg_bytes = MODE == Mode::Forward ? 4 * M * B : 4 * (PAD + NN) * B;
-    static constexpr int acc = align16(vg + vg_bytes);               // double[NW][2*NOUT]
+    static constexpr int vg_bytes = MODE == Mode::Forward ? 4 * M * B : 4 * (VPAD + NN) * B;
+    // LMM_TPP_VCOMP: the vega rows' Kahan compensations, BF16 [VPAD+NN][B].
+    static constexpr int vc = vg + vg_bytes;
+    static constexpr int vc_bytes = (LMM_TPP_VCOMP && MODE != Mode::Forward) ? 2 * (VPAD + NN) * B : 0;
+    static constexpr int acc = align16(vc + vc_bytes);               // double[NW][2*NOUT]
     static constexpr int bytes = acc + 8 * NW * 2 * NOUT;
 };
 
@@ -247,11 +266,68 @@ __device__ __forceinline__ void fwd_pair_window(float (&IL)[NN], const float4 *k
     fwd_cell(IL[NN - 1], V1, C[(NN - 2) % R], sqez1, delta);
 }
 
+// Forward steps n .. n+G-1 with one body over positions p (ascending): cell
+// (n+g, p-g) for g = 0..G-1, which finds IL_{n+g,p-g} written by cell
+// (n+g-1, p-g) one position earlier, so the G drift chains are independent
+// within a position. Cell (n+g, p-g) has k = p-n-1-2g, the constants of
+// position j = p-2g of step n: ring C of 2G-1+P slots, each constant loaded
+// once per G cells, P positions ahead of its first use. Entered at the chunk
+// holding rate n+1; cells of step n+g below its first active rate n+g+1 see
+// zero constants and are exact no-ops. V[g] returns step n+g's drift sum.
+template <int NN, int CH, int P, int G>
+__device__ __forceinline__ void fwd_group_window(float (&IL)[NN], const float4 *kcn, const float (&sqez)[G],
+                                                 float delta, int n, float (&V)[G])
+{
+    constexpr int R = 2 * G - 1 + P;
+#define LMM_RING(j) ((((j) % R) + R) % R)
+    float4 C[R];
+#pragma unroll
+    for (int g = 0; g < G; ++g) V[g] = drift0(sqez[g]);
+    const int c0 = (n + 1) / CH;
+#pragma unroll
+    for (int c = 0; c * CH < NN; ++c) {
+        if (c >= c0) {
+            if (c == c0) {
+#pragma unroll
+                for (int j = c * CH - 2 * (G - 1); j < c * CH + P; ++j)
+                    if (j >= -(G - 1) * 2 && j < NN) C[LMM_RING(j)] = kcn[j];
+            }
+#pragma unroll
+            for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
+                if (p + P < NN) C[LMM_RING(p + P)] = kcn[p + P];
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+                    if (p - g >= 1) fwd_cell(IL[p - g], V[g], C[LMM_RING(p - 2 * g)], sqez[g], delta);
+            }
+        }
+    }
+    // the trailing steps' last cells, positions NN .. NN+G-2
+#pragma unroll
+    for (int p = NN; p < NN + G - 1; ++p) {
+#pragma unroll
+        for (int g = p - NN + 1; g < G; ++g) fwd_cell(IL[p - g], V[g], C[LMM_RING(p - 2 * g)], sqez[g], delta);
+    }
+#undef LMM_RING
+}
+
 struct RevStep {
     float V, S, sqez;   // drift sum, delta^2 times the reference's v1, sqrt(delta) z
     const float4 *kc;   // kc[i]: constants of k = i-n-1
     float *vg;          // vg[i*B]: this thread's vega slot of k = i-n-1
+    unsigned short *vc; // vc[i*B]: its BF16 compensation (LMM_TPP_VCOMP)
 };
+
+__device__ __forceinline__ float bf16_bits_to_float(unsigned short b) { return __uint_as_float((unsigned)b << 16); }
+
+// Kahan step s += x with the compensation c held as BF16 bits: c is the
+// negated rounding error of the previous additions, so s - c is the sum.
+__device__ __forceinline__ void kahan_add_bf16c(float &s, unsigned short &cb, float x)
+{
+    const float y = __fsub_rn(x, bf16_bits_to_float(cb));
+    const float t = __fadd_rn(s, y);
+    cb = __bfloat16_as_ushort(__float2bfloat16_rn(__fsub_rn(__fsub_rn(t, s), y)));
+    s = t;
+}
 
 // One reverse cell (path_calc_b2 :105-111 in log-adjoint form) + vega, with
 // its constants and vega partial sum passed in from the window.
@@ -294,6 +370,7 @@ __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN
     constexpr int W = 2 * G - 1 + P;
     const float4 *kc = st[0].kc;
     float *vg = st[0].vg;
+    unsigned short *vc = st[0].vc;
     float4 C[W];
     float A[W];
 #pragma unroll
@@ -318,7 +395,12 @@ __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN
                 }
             }
             const int jf = i + 2 * (G - 1);
-            if (jf >= 1 && jf <= JMAX) vg[jf * B] += A[jf % W];
+            if (jf >= 1 && jf <= JMAX) {
+                if (LMM_TPP_VCOMP)
+                    kahan_add_bf16c(vg[jf * B], vc[jf * B], A[jf % W]);
+                else
+                    vg[jf * B] += A[jf % W];
+            }
         }
     }
 }
@@ -415,21 +497,27 @@ __device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb
 
 // Column sums of a warp's 32 shared-memory columns: lane handles outputs
 // k = lane, lane+32, ...; the (t+lane)&31 rotation keeps the 32 lanes on 32
-// different banks. Adds sums and sums of squares into FP64 accumulators.
+// different banks. Adds sums (TwoSum-compensated, LMM_COMP_SUMS) and sums of
+// squares into FP64 accumulators; vc: the rows' BF16 Kahan compensations.
 template <int NN, int B>
 __device__ __forceinline__ void column_reduce(const float *vg, int warp, int lane, double *acc,
-                                              int nout, int off)
+                                              int nout, int off, const unsigned short *vc = nullptr)
 {
     for (int k = lane; k < NN; k += 32) {
         const float *col = vg + k * B + warp * 32;
-        float a = 0.0f, a2 = 0.0f;
+        const unsigned short *ccol = vc ? vc + k * B + warp * 32 : nullptr;
+        float a = 0.0f, c = 0.0f, a2 = 0.0f;
 #pragma unroll 8
         for (int t = 0; t < 32; ++t) {
-            const float x = col[(t + lane) & 31];
-            a += x;
+            const float x = ccol ? __fsub_rn(col[(t + lane) & 31], bf16_bits_to_float(ccol[(t + lane) & 31]))
+                                 : col[(t + lane) & 31];
+            if (LMM_COMP_SUMS)
+                two_sum_acc(a, c, x);
+            else
+                a += x;
             a2 = fmaf(x, x, a2);
         }
-        acc[off + k] += (double)a;
+        acc[off + k] += (double)a + (double)c;
         acc[nout + off + k] += (double)a2;
     }
 }
@@ -444,7 +532,19 @@ __device__ __forceinline__ void forward_all(float (&IL)[NN], const float4 *kc0, 
                                             float *tape_v, int64_t total, bool active)
 {
     constexpr int B = tpp_block<MODE>();
-    if constexpr (MODE == Mode::Fused) {
+    if constexpr (MODE == Mode::Fused && LMM_TPP_FGROUP == 4) {
+        static_assert(NMAT % 4 == 0, "forward steps in groups of four");
+        for (int n = 0; n < NMAT; n += 4) {
+            if (LMM_TPP_SYNC) __syncthreads();
+            zq = zq_next;
+            if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+            const float sqez[4] = {sqd * zq.x, sqd * zq.y, sqd * zq.z, sqd * zq.w};
+            float V[4];
+            fwd_group_window<NN, LMM_TPP_CHUNK, kPref<PHILOX>, 4>(IL, kc0 - (n + 1), sqez, delta, n, V);
+#pragma unroll
+            for (int g = 0; g < 4; ++g) vt_s[(n + g) * B] = V[g];
+        }
+    } else if constexpr (MODE == Mode::Fused) {
         static_assert(NMAT % 2 == 0, "paired forward steps");
         for (int n = 0; n < NMAT; n += 2) {
             if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0) __syncthreads();
@@ -475,12 +575,14 @@ __device__ __forceinline__ void forward_all(float (&IL)[NN], const float4 *kc0, 
 // Reverse over all steps, in groups of G steps from the last.
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
 __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], const float4 *kc0,
-                                            float *vg0, float4 &zq, float4 &zq_next, const float *zp,
+                                            float *vg0, unsigned short *vc0, float4 &zq, float4 &zq_next, const float *zp,
                                             uint64_t seed, uint64_t gpath, float sqd, float delta,
                                             const float *vt_s, const float *tape_v, int64_t total)
 {
     constexpr int G = MODE == Mode::Fused ? LMM_TPP_SKEW : LMM_TPP_SKEW_BWD;
     static_assert(NMAT % G == 0 && (G == 2 || G == 4), "whole step groups");
+    constexpr int RCH = PHILOX ? LMM_TPP_RCHUNK_PHILOX : LMM_TPP_RCHUNK;
+    static_assert(RCH - 1 <= TppLayout<NN, NMAT, MODE>::VPAD, "the windows' spare vega rows lie inside the table");
     constexpr int B = tpp_block<MODE>();
     for (int n = NMAT - 1; n > 0; n -= G) {
         if (LMM_TPP_SYNC) __syncthreads();
@@ -501,9 +603,9 @@ __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], co
             st[g].S = 0.0f;
             st[g].kc = kc0 - (m + 1);
             st[g].vg = vg0 - (m + 1) * B;
+            st[g].vc = vc0 - (m + 1) * B;
         }
-        rev_group_window<NN, B, G, (PHILOX ? LMM_TPP_RCHUNK_PHILOX : LMM_TPP_RCHUNK), kPref<PHILOX>>(IL, Pb, st,
-                                                                                                   delta, n);
+        rev_group_window<NN, B, G, RCH, kPref<PHILOX>>(IL, Pb, st, delta, n);
     }
 }
 
@@ -542,7 +644,9 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     const float delta = m.delta, sqd = m.sqd;
     const int64_t total = (int64_t)m.nscen * w.paths;
     const float4 *kc0 = kc_s + PAD;
-    float *vg0 = vg_s + PAD * B + tid;
+    float *vg0 = vg_s + Lay::VPAD * B + tid;
+    unsigned short *vc_s = reinterpret_cast<unsigned short *>(smem + Lay::vc);
+    unsigned short *vc0 = vc_s + Lay::VPAD * B + tid;
     float *vt0 = vt_s + tid;
 
     // Units (scenario, item) in a block-stride loop: with a grid of one wave,
@@ -602,8 +706,12 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 payoff_adjoint<NN, NMAT, B>(IL, Pb, vb, V, disc, Bst, ILst, mask, delta, ost_s, okf_s, owf_s);
 #pragma unroll
                 for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+                if (LMM_TPP_VCOMP) {
+#pragma unroll
+                    for (int k = 0; k < NN; ++k) vc0[k * B] = 0;
+                }
                 if (!kYrun) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, NMAT / 4 - 1);
-                reverse_all<NN, NMAT, PHILOX, MODE>(IL, Pb, kc0, vg0, zq, zq_next, zp, seed, gpath, sqd, delta,
+                reverse_all<NN, NMAT, PHILOX, MODE>(IL, Pb, kc0, vg0, vc0, zq, zq_next, zp, seed, gpath, sqd, delta,
                                                     vt0, tape_v, total);
             }
 
@@ -619,13 +727,17 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             if (MODE != Mode::Forward) {
                 constexpr int voff = MODE == Mode::Fused ? 1 + NN : NN;
                 constexpr int doff = MODE == Mode::Fused ? 1 : 0;
-                float *vgw = vg_s + PAD * B;
+                float *vgw = vg_s + Lay::VPAD * B;
                 if (!active) {
 #pragma unroll
                     for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+                    if (LMM_TPP_VCOMP) {
+#pragma unroll
+                        for (int k = 0; k < NN; ++k) vc0[k * B] = 0;
+                    }
                 }
                 __syncwarp();
-                column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, voff);
+                column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, voff, LMM_TPP_VCOMP ? vc_s + Lay::VPAD * B : nullptr);
                 __syncwarp();
 #pragma unroll
                 for (int i = 0; i < NN; ++i) vg0[i * B] = active ? Pb[i] * il0_s[i] : 0.0f;
