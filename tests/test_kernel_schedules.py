@@ -109,6 +109,103 @@ def test_forward_hand_over_matches_the_steps_each_half_runs():
             written[r % 2] = (2 * r, 2 * r + 1)
 
 
+# The fused two-threads-per-path kernel cuts the rates into blocks of L and
+# the two roles own alternate blocks; block s runs forward steps 2(r-s),
+# 2(r-s)+1 in round r and reverse steps n, n-1 with n = NMAT-1-2(r-(S-1-s)).
+# The window rules per block are those above with the block's L rates and a
+# chunk of 8 rates (4 when L is not a multiple of 8).
+def blk_rev_window(L, lo, n):
+    """Vega rows (as k) flushed and constant rows (as k) loaded by the reverse
+    window of steps n, n-1 over the block of L rates from rate lo."""
+    ch = 8 if L % 8 == 0 else 4
+    jmax = L + G - 2
+    imin = n - 1 - lo
+    slots, consts = set(), set()
+    if imin >= L:
+        return set(), set()
+    consts.update(range(L - P, jmax + 1))
+    completed = True
+    q = 0
+    while q * ch < L + G - 1:
+        top = L - 1 - q * ch
+        if top < imin:
+            completed = False
+            break
+        i = top
+        while i > top - ch and i >= -(G - 1):
+            if i - P >= 0:
+                consts.add(i - P)
+            jf = i + 2 * (G - 1)
+            if 0 <= jf <= jmax:
+                slots.add(jf)
+            i -= 1
+        q += 1
+    if completed:
+        slots.add(0)
+    to_k = lambda j: lo + j - n - 1
+    return {to_k(j) for j in slots}, {to_k(j) for j in consts}
+
+
+@pytest.mark.parametrize("L", [80, 40, 20])
+def test_block_rounds_touch_disjoint_vega_rows_and_stay_in_the_tables(L):
+    """In every reverse round the rows the blocks flush are pairwise disjoint
+    between the two roles' blocks (each role runs its own blocks one after
+    another), and every row and constant lies inside the tables."""
+    S = NN // L
+    for r in range(NMAT // 2 + S - 1):
+        per_role = {0: [], 1: []}
+        for s in range(S):
+            jr = r - (S - 1 - s)
+            if not 0 <= jr < NMAT // 2:
+                continue
+            n = NMAT - 1 - 2 * jr
+            rows, consts = blk_rev_window(L, s * L, n)
+            assert all(-VPAD <= k <= NN - 1 for k in rows), (L, r, s, min(rows))
+            assert all(-PADK <= k <= NN - 1 for k in consts), (L, r, s)
+            per_role[s % 2].append(rows)
+        a = set().union(*per_role[0]) if per_role[0] else set()
+        b = set().union(*per_role[1]) if per_role[1] else set()
+        assert not (a & b), (L, r, sorted(a & b))
+
+
+@pytest.mark.parametrize("L", [80, 40, 20])
+def test_block_reverse_flushes_every_active_cell(L):
+    """Each active cell (n', i) adds to row k = i - n' - 1: the block holding
+    rate i, in the round it runs step n', flushes that row."""
+    S = NN // L
+    for s in range(S):
+        for jr in range(NMAT // 2):
+            n = NMAT - 1 - 2 * jr
+            rows, _ = blk_rev_window(L, s * L, n)
+            for step in (n, n - 1):
+                for i in range(max(step + 1, s * L), (s + 1) * L):
+                    assert i - step - 1 in rows, (L, s, n, step, i)
+
+
+@pytest.mark.parametrize("L", [80, 40, 20])
+def test_block_hand_overs_match_the_steps_each_block_runs(L):
+    """Forward: block s reads in round r the buffer (s-1, (r-1) % 2) that block
+    s-1 wrote in round r-1 for the same steps, and block s-1 writes that
+    buffer again only in round r+1. Reverse: the same downwards."""
+    S = NN // L
+    fw, rv = {}, {}
+    for r in range(NMAT // 2 + S - 1):
+        for s in range(S):
+            n = 2 * (r - s)
+            if 0 <= n < NMAT:
+                if s > 0:
+                    assert fw[(s - 1, (r - 1) % 2)] == (r - 1, n), (L, r, s)
+                if s < S - 1:
+                    fw[(s, r % 2)] = (r, n)
+            jr = r - (S - 1 - s)
+            if 0 <= jr < NMAT // 2:
+                n = NMAT - 1 - 2 * jr
+                if s < S - 1:
+                    assert rv[(s, (r - 1) % 2)] == (r - 1, n), (L, r, s)
+                if s > 0:
+                    rv[(s - 1, r % 2)] = (r, n)
+
+
 # The thread-per-path kernel (csrc/lmm_f32_tpp.cu) leaves its reverse body
 # early in the same way: a group of G steps n, n-1, ..., n-G+1 runs positions
 # from the top in chunks and returns at the first chunk wholly below its
