@@ -372,6 +372,7 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                                                : tape + (int64_t)(NN + NMAT) * total + tp;
             const int ck = MODE == Mode::Fused ? m.ckpt : 0;
             const int NCK = tp2_nckpt(NMAT, ck);
+            const int ckd = ck > 0 ? ck : 1;             // divisor of the checkpoint tests (used when NCK > 0)
             // checkpoint c (the rates after step (c+1) ck - 1), rate i: ckp[(c*NN + i)*PB]
             float *ckp = tape + (int64_t)gridDim.x * (S - 1) * NMAT * PB + (int64_t)blockIdx.x * NCK * NN * PB + ps;
 
@@ -426,9 +427,9 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                         tape_v[(int64_t)n * total] = Y0;
                         tape_v[(int64_t)(n + 1) * total] = Y1;
                     }
-                    if (NCK > 0 && (n + 2) % ck == 0 && n + 2 < NMAT) {
+                    if (NCK > 0 && (n + 2) % ckd == 0 && n + 2 < NMAT) {
                         // rates i <= n+2 are final from here on: only the others are saved
-                        const int c = (n + 2) / ck - 1;
+                        const int c = (n + 2) / ckd - 1;
 #pragma unroll
                         for (int p = 0; p < L; ++p)
                             if (lo + p > n + 2) ckp[(c * NN + lo + p) * PB] = X[q * L + p];
@@ -574,9 +575,9 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                     if (imin < L)
                         tp2_rev_block<H, L, PB, CH, P>(q, X, Pb, st, kc_s + PADK + lo - (n + 1),
                                                        vg0 + (lo - n - 1) * PB, delta, imin);
-                    if (NCK > 0 && (n - 1) % ck == 0 && n - 1 >= ck) {
+                    if (NCK > 0 && (n - 1) % ckd == 0 && n - 1 >= ck) {
                         // the reverse of steps >= n-1 leaves rates i <= n-1 untouched
-                        const int c = (n - 1) / ck - 1;
+                        const int c = (n - 1) / ckd - 1;
 #pragma unroll
                         for (int p = 0; p < L; ++p)
                             if (lo + p > n - 1) X[q * L + p] = ckp[(c * NN + lo + p) * PB];
