@@ -17,9 +17,10 @@
 // register j holds rate (2(j/L) + role) L + j%L. Step n moves only the rates
 // above n, so with two halves (L = H) the lower half runs out of work after
 // step H-1 while the upper half stays busy: at 160/120 the halves own 3,160
-// and 8,780 cells. Alternating blocks of L = 20 share the cells of every
-// step between the roles (one round-cost model of the skewed schedule below:
-// 8,937 -> 6,670, ideal 5,970).
+// and 8,780 cells. Alternating blocks share the cells of every step between
+// the roles (a round-cost model of the skewed schedule below, the sum over
+// rounds of the busier role's cells: two halves 8,937; blocks of 40 7,326;
+// of 20 6,670; ideal 5,970).
 //
 // The drift sum of a step runs upwards over i, the adjoint's suffix sum and
 // the drift reconstruction downwards, so the blocks form a pipeline worked in
@@ -53,10 +54,12 @@
 // rows; drift sums carry the normal term (Y = V + sqrt(delta) z).
 #include "lmm_device.cuh"
 
-// Rates per block of the fused kernel (20: four blocks per thread at
-// NN=160; 80: the two halves).
+// Rates per block of the fused kernel (40: two blocks per thread at NN=160;
+// 80: the two halves). GB300, 160/120, 1,048,576 paths: blocks of 20 / 40 /
+// 80 rates 25.6 / 18.3 / 20.4 ms: blocks of 20 lose more to the per-block
+// window set-up and hand-overs than the better balance gains.
 #ifndef LMM_TP2_SEG
-#define LMM_TP2_SEG 20
+#define LMM_TP2_SEG 40
 #endif
 
 namespace lmm {

@@ -27,11 +27,12 @@ def P():
 
 @pytest.mark.parametrize("k", [0, 4, 8, 16])
 def test_long_tenor_interval_matches_oracle(P, k):
-    """160x120 (two threads per path), 30 swaptions, random curve and vols in
-    0.1..0.3: rates restored every k steps (0: never)."""
+    """160x120 (two threads per path), 30 swaptions, random curve and vols:
+    rates restored every k steps (0: never), on the same normals for every k
+    (those of test_long_tenor_checkpointed_fp32_matches_oracle)."""
     cfg = cfgs().workload(3, 512)
     cfg.ckpt_every = k
-    z = O.normals_f32(9100 + k, cfg.paths, cfg.nmat)
+    z = O.normals_f32(303, cfg.paths, cfg.nmat)
     with P.Engine(cfg) as e:
         assert e.checkpoint_interval == k
         g, _ = e.greeks_f32(z)
@@ -44,7 +45,7 @@ def test_warp_per_path_interval_matches_oracle(P, k):
     """A warp-per-path shape (200x100): rates restored every k steps."""
     cfg = _random_cfg(200, 100, 12, 200 * 1000 + 100, 384)
     cfg.ckpt_every = k
-    z = O.normals_f32(9200 + k, cfg.paths, cfg.nmat)
+    z = O.normals_f32(9200, cfg.paths, cfg.nmat)
     with P.Engine(cfg) as e:
         g, _ = e.greeks_f32(z)
     m, _ = O.greeks(cfg, z.astype(np.float64))
