@@ -126,17 +126,6 @@
 #ifndef LMM_TPP_VCOMP
 #define LMM_TPP_VCOMP 0
 #endif
-// 1: the fused kernel's step barriers hold its two groups of four warps
-// apart (named barriers 1 and 2; each scheduler runs one warp of each group)
-// and the second group starts LMM_TPP_PHASE_NS later, so that one group's
-// forward (special-function bound) runs beside the other's reverse (issue
-// bound). 0: one barrier for the whole block.
-#ifndef LMM_TPP_PHASE
-#define LMM_TPP_PHASE 0
-#endif
-#ifndef LMM_TPP_PHASE_NS
-#define LMM_TPP_PHASE_NS 35000
-#endif
 // Positions ahead at which the step windows load the constants of a rate
 // from shared memory (0: at the position that first uses them), with the
 // normals read from memory and with Philox normals (more live registers).
@@ -205,19 +194,6 @@ __device__ __forceinline__ float pick4(const float4 &q, int j)
     r = j == 2 ? q.z : r;
     r = j == 3 ? q.w : r;
     return r;
-}
-
-// Barrier of the step loops: the whole block, or (fused kernel with
-// LMM_TPP_PHASE) the thread's group of four warps.
-template <Mode MODE>
-__device__ __forceinline__ void step_sync()
-{
-    if (MODE == Mode::Fused && LMM_TPP_PHASE) {
-        static_assert(MODE != Mode::Fused || !LMM_TPP_PHASE || LMM_TPP_BLOCK == 256, "two groups of 128 threads");
-        asm volatile("bar.sync %0, 128;\n" ::"r"(1 + (int)(threadIdx.x >> 7)) : "memory");
-    } else {
-        __syncthreads();
-    }
 }
 
 // Running drift sum at the start of a step: V = 0, or Y = sqrt(delta) z.
@@ -513,7 +489,7 @@ __device__ __forceinline__ void forward_all(float (&IL)[NN], const float4 *kc0, 
     if constexpr (MODE == Mode::Fused) {
         static_assert(NMAT % 2 == 0, "paired forward steps");
         for (int n = 0; n < NMAT; n += 2) {
-            if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0) step_sync<MODE>();
+            if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0) __syncthreads();
             if ((n & 3) == 0) {
                 zq = zq_next;
                 if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
@@ -551,7 +527,7 @@ __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], co
     static_assert(RCH - 1 <= TppLayout<NN, NMAT, MODE>::VPAD, "the windows' spare vega rows lie inside the table");
     constexpr int B = tpp_block<MODE>();
     for (int n = NMAT - 1; n > 0; n -= G) {
-        if (LMM_TPP_SYNC) step_sync<MODE>();
+        if (LMM_TPP_SYNC) __syncthreads();
         // The drift sums carry the normal term (kYrun): the reverse needs no
         // normals. Skipped explicitly: left to the compiler, the unused
         // loads and Philox evaluations stayed in (GB300, 4,194,304 paths:
@@ -628,7 +604,6 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         for (int i = tid; i < Lay::NW * 2 * NOUT; i += B) acc_s[i] = 0.0;
         __syncthreads();
 
-        if (MODE == Mode::Fused && LMM_TPP_PHASE && (tid >> 7) == 1) __nanosleep(LMM_TPP_PHASE_NS);
         const int64_t ibase = (int64_t)item * w.ppt * B;
         const float vb = MODE == Mode::Backward ? (float)vbar[scen] : 1.0f;
         for (int j = 0; j < w.ppt; ++j) {
