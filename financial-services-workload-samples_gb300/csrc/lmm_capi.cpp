@@ -114,6 +114,7 @@ struct lmm_engine {
     DevBuf partial, z32, z64, out, se, flag, vbar;
     DevBuf wscratch;               // warp-per-path kernels: Y_top per warp, step and lane
     DevBuf bumpvar;                // central bumps: the variants' means and standard errors
+    std::vector<float4> kc_host;   // the per-maturity constants, host copy
     std::map<int, int> bps;        // cached blocks per SM per kernel variant
     int32_t last_launches = 0;
     bool timing = false;
@@ -574,6 +575,8 @@ int lmm_engine_create(const lmm_params *p, int32_t device, lmm_engine **out)
     m.deltad = d;
     m.sqdd = std::sqrt(d);
     m.kc = reinterpret_cast<const float4 *>(base + o_kc);
+    e->kc_host = kc;
+    m.kc_host = e->kc_host.data();
     m.L0f = reinterpret_cast<const float *>(base + o_l0f);
     m.invL0f = reinterpret_cast<const float *>(base + o_il0f);
     m.L0d = reinterpret_cast<const double *>(base + o_l0d);

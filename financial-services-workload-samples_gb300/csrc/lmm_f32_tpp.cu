@@ -126,6 +126,11 @@
 #ifndef LMM_TPP_VCOMP
 #define LMM_TPP_VCOMP 0
 #endif
+// 1: the per-maturity constants travel as a kernel parameter and the step
+// windows read them from the parameter (constant) bank; 0: from shared memory.
+#ifndef LMM_TPP_KCPARAM
+#define LMM_TPP_KCPARAM 1
+#endif
 // Positions ahead at which the step windows load the constants of a rate
 // from shared memory (0: at the position that first uses them), with the
 // normals read from memory and with Philox normals (more live registers).
@@ -551,10 +556,17 @@ __device__ __forceinline__ void reverse_all(float (&IL)[NN], float (&Pb)[NN], co
     }
 }
 
+// The per-maturity constants with NMAT zero rows in front (k = i-n-1 < 0),
+// passed by value as a kernel parameter.
+template <int NN, int NMAT>
+struct TppConst {
+    float4 v[NMAT + NN];
+};
+
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
 __global__ void __launch_bounds__(tpp_block<MODE>(), tpp_min_blocks<MODE>())
 k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
-      float *__restrict__ tape, const double *__restrict__ vbar)
+      float *__restrict__ tape, const double *__restrict__ vbar, const __grid_constant__ TppConst<NN, NMAT> kp)
 {
     using Lay = TppLayout<NN, NMAT, MODE>;
     constexpr int B = Lay::B, M = Lay::M, NOUT = Lay::NOUT, PAD = Lay::PAD;
@@ -572,9 +584,11 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < PAD + NN; i += B) {
-        const int k = i - PAD;
-        kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
+    if (!LMM_TPP_KCPARAM) {
+        for (int i = tid; i < PAD + NN; i += B) {
+            const int k = i - PAD;
+            kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
+        }
     }
     for (int i = tid; i <= M; i += B) ost_s[i] = m.opt_start[i];
     for (int i = tid; i < m.nopt; i += B) {
@@ -585,7 +599,7 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     double *acc = acc_s + warp * 2 * NOUT;
     const float delta = m.delta, sqd = m.sqd;
     const int64_t total = (int64_t)m.nscen * w.paths;
-    const float4 *kc0 = kc_s + PAD;
+    const float4 *kc0 = (LMM_TPP_KCPARAM ? kp.v : kc_s) + PAD;
     float *vg0 = vg_s + Lay::VPAD * B + tid;
     unsigned short *vc_s = reinterpret_cast<unsigned short *>(smem + Lay::vc);
     unsigned short *vc0 = vc_s + Lay::VPAD * B + tid;
@@ -707,8 +721,11 @@ cudaError_t launch_tpp(const DevModel &m, const float *z, uint64_t seed, int64_t
     auto kern = k_tpp<NN, NMAT, PHILOX, MODE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
     if (e != cudaSuccess) return e;
+    TppConst<NN, NMAT> kp;
+    for (int i = 0; i < NMAT + NN; ++i)
+        kp.v[i] = i < NMAT ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc_host[i - NMAT];
     const unsigned grid = (unsigned)(w.grid > 0 ? w.grid : (int64_t)m.nscen * w.items);
-    kern<<<grid, Lay::B, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar);
+    kern<<<grid, Lay::B, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar, kp);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,8 @@ struct DevModel {
     float delta, sqd, d2;                 // delta, sqrt(delta), delta^2
     double deltad, sqdd;
     const float4 *kc;                     // [nn]
+    const float4 *kc_host;                // [nn] the same constants in host memory, for
+                                          // launches that pass them as kernel parameters
     const float *L0f;                     // [nscen][nn]
     const float *invL0f;                  // [nscen][nn]
     const double *L0d;                    // [nscen][nn]

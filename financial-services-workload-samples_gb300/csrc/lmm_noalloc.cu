@@ -222,6 +222,7 @@ extern "C" int lmm_greeks_f32_device_noalloc(const lmm_params *p, const float *d
     m.deltad = d;
     m.sqdd = std::sqrt(d);
     m.kc = dmod->kc;
+    m.kc_host = hm.kc;
     m.L0f = dmod->L0f;
     m.invL0f = dmod->iL0f;
     m.L0d = dmod->L0d;
