@@ -126,8 +126,11 @@
 #ifndef LMM_TPP_VCOMP
 #define LMM_TPP_VCOMP 0
 #endif
-// 1: the per-maturity constants travel as a kernel parameter and the step
-// windows read them from the parameter (constant) bank; 0: from shared memory.
+// 1: in the fused kernel the per-maturity constants travel as a kernel
+// parameter and the step windows read them from the parameter (constant)
+// bank; 0: from shared memory. GB300, 4,194,304 paths: 11.04 -> 10.85 ms
+// (232 instead of 252 registers); the forward-only and backward-only kernels
+// ran slower that way (3.75 -> 4.82 and 9.07 -> 9.41 ms) and keep shared memory.
 #ifndef LMM_TPP_KCPARAM
 #define LMM_TPP_KCPARAM 1
 #endif
@@ -584,7 +587,8 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (!LMM_TPP_KCPARAM) {
+    constexpr bool kKcParam = LMM_TPP_KCPARAM && MODE == Mode::Fused;
+    if (!kKcParam) {
         for (int i = tid; i < PAD + NN; i += B) {
             const int k = i - PAD;
             kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
@@ -599,7 +603,7 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     double *acc = acc_s + warp * 2 * NOUT;
     const float delta = m.delta, sqd = m.sqd;
     const int64_t total = (int64_t)m.nscen * w.paths;
-    const float4 *kc0 = (LMM_TPP_KCPARAM ? kp.v : kc_s) + PAD;
+    const float4 *kc0 = (kKcParam ? kp.v : kc_s) + PAD;
     float *vg0 = vg_s + Lay::VPAD * B + tid;
     unsigned short *vc_s = reinterpret_cast<unsigned short *>(smem + Lay::vc);
     unsigned short *vc0 = vc_s + Lay::VPAD * B + tid;
