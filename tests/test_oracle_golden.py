@@ -112,3 +112,14 @@ def test_reference_work_port_matches_oracle():
     v, d = O.reference_work(cfg, z, 256)
     m, _ = O.greeks(cfg, z)
     assert v == pytest.approx(m[0], rel=1e-13) and d == pytest.approx(m[cfg.nn], rel=1e-13)
+
+
+def test_tuned_cpu_baseline_build_computes_the_same_work():
+    """The timed CPU baseline (the oracle's source under the reference-like
+    fast-math flags) returns the checker's value and last delta to rounding:
+    it times the same work, not a different one."""
+    cfg = cfgs().workload(2, 4096)
+    z = O.normals_f64(5, 4096, 40)
+    v, d = O.reference_work(cfg, z, 4096, build="checker")
+    vt, dt = O.reference_work(cfg, z, 4096, build="tuned")
+    assert vt == pytest.approx(v, rel=1e-10) and dt == pytest.approx(d, rel=1e-9)
