@@ -863,7 +863,10 @@ int lmm_swaption_breakdown_f64_device(lmm_engine *e, const double *d_z, int64_t 
 // whole device waves: 363 -> 369 M paths/s; {1,3,10,22}/36: 369 -> 373 M
 // paths/s. Each piece writes its own range of partial sums and one ordered
 // k_finalize covers them all. Single-scenario engines only.
-constexpr int kHostSplit[] = {1, 3, 10, 22};
+#ifndef LMM_HOST_SPLIT
+#define LMM_HOST_SPLIT 1, 3, 10, 22
+#endif
+constexpr int kHostSplit[] = {LMM_HOST_SPLIT};
 constexpr int kHostChunks = sizeof(kHostSplit) / sizeof(kHostSplit[0]);
 static_assert(kHostChunks <= 8, "one copy event per piece");
 constexpr int64_t kPipelineMinPaths = int64_t(1) << 18;
