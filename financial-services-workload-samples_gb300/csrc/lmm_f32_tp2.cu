@@ -61,11 +61,6 @@
 #ifndef LMM_TP2_SEG
 #define LMM_TP2_SEG 40
 #endif
-// 1: the fused kernel reads the per-maturity constants from a kernel
-// parameter (the constant bank); 0: from shared memory.
-#ifndef LMM_TP2_KCPARAM
-#define LMM_TP2_KCPARAM 0
-#endif
 
 namespace lmm {
 namespace {
@@ -297,12 +292,6 @@ __device__ __forceinline__ void tp2_rows_reduce(const float *rows0, int lane, in
     }
 }
 
-// The per-maturity constants with NMAT zero rows in front, by value.
-template <int NN, int NMAT>
-struct Tp2Const {
-    float4 v[NMAT + NN];
-};
-
 // MODE Fused: value + Greeks; `tape` is the launch's scratch: [grid][S-1][NMAT][PB]
 // drift sums at the top rate of every block but the last, then
 // [grid][tp2_nckpt][NN][PB] rate checkpoints, one every m.ckpt steps.
@@ -313,7 +302,7 @@ struct Tp2Const {
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
 __global__ void __launch_bounds__(Tp2Shape<NN>::kBlock, Tp2Shape<NN>::kMinBlocks)
 k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
-      float *__restrict__ tape, const double *__restrict__ vbar, const __grid_constant__ Tp2Const<NN, NMAT> kp)
+      float *__restrict__ tape, const double *__restrict__ vbar)
 {
     using Lay = Tp2Layout<NN, NMAT, MODE>;
     constexpr int H = Lay::H, PB = Lay::PB, M = Lay::M, NOUT = Lay::NOUT, PADK = Lay::PADK;
@@ -343,14 +332,10 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     // so each scheduler gets one warp of each.
     const int role = (warp & 1) ^ (LMM_TP2_SWIZZLE ? (warp >> 2) & 1 : 0), pair = warp >> 1;
     const int ps = pair * 32 + lane;                 // path slot in the batch
-    constexpr bool kKcParam = LMM_TP2_KCPARAM && MODE == Mode::Fused;
-    if (!kKcParam) {
-        for (int i = tid; i < PADK + NN; i += Lay::B) {
-            const int k = i - PADK;
-            kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
-        }
+    for (int i = tid; i < PADK + NN; i += Lay::B) {
+        const int k = i - PADK;
+        kc_s[i] = k < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc[k];
     }
-    const float4 *kcb = kKcParam ? kp.v : kc_s;      // kcb[PADK + k]: constants of k
     for (int i = tid; i <= M; i += Lay::B) ost_s[i] = m.opt_start[i];
     for (int i = tid; i < m.nopt; i += Lay::B) {
         okf_s[i] = m.optKf[i];
@@ -427,7 +412,7 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                     const int first = n + 1 - lo;            // step n's first active rate in the block
                     if (first < L) {
                         const int c0 = first > 0 ? first / CH : 0;
-                        tp2_fwd_block<H, L, CH, P>(q, X, kcb + PADK + lo - (n + 1), c0, delta, Y0, Y1);
+                        tp2_fwd_block<H, L, CH, P>(q, X, kc_s + PADK + lo - (n + 1), c0, delta, Y0, Y1);
                     }
                     if (s < S - 1) {
                         float *h = hf_s + (s * 2 + (r & 1)) * 2 * PB + ps;
@@ -591,7 +576,7 @@ k_tp2(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                     }
                     const int imin = n - 1 - lo;             // lowest position with an active cell
                     if (imin < L)
-                        tp2_rev_block<H, L, PB, CH, P>(q, X, Pb, st, kcb + PADK + lo - (n + 1),
+                        tp2_rev_block<H, L, PB, CH, P>(q, X, Pb, st, kc_s + PADK + lo - (n + 1),
                                                        vg0 + (lo - n - 1) * PB, delta, imin);
                     if (NCK > 0 && (n - 1) % ckd == 0 && n - 1 >= ck) {
                         // the reverse of steps >= n-1 leaves rates i <= n-1 untouched
@@ -657,11 +642,8 @@ cudaError_t launch_tp2(const DevModel &m, const float *z, uint64_t seed, int64_t
     auto kern = k_tp2<NN, NMAT, PHILOX, MODE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
     if (e != cudaSuccess) return e;
-    Tp2Const<NN, NMAT> kp;
-    for (int i = 0; i < NMAT + NN; ++i)
-        kp.v[i] = i < NMAT ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc_host[i - NMAT];
     const unsigned grid = (unsigned)(w.grid > 0 ? w.grid : (int64_t)m.nscen * w.items);
-    kern<<<grid, Lay::B, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar, kp);
+    kern<<<grid, Lay::B, Lay::bytes, s>>>(m, z, seed, path0, w, tape, vbar);
     return cudaGetLastError();
 }
 
