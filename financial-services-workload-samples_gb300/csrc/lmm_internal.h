@@ -67,9 +67,9 @@ cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_
 // [nmat][total] full drift sums, [nmat][total] drift sums at rate nn/2 - 1.
 bool f32_tp2_supports(int nn, int nmat);
 int tp2_paths_per_block(int nn);
-// Scratch of the fused kernel per block (floats): the lower half's drift sums
-// at the half boundary per step, and both halves' rate checkpoints, one every
-// ckpt steps (ckpt even; 0: none).
+// Scratch of the fused kernel per block (floats): the drift sums at the top
+// rate of every rate block but the last, per step, and the rate checkpoints,
+// one every ckpt steps (ckpt even; 0: none).
 size_t tp2_scratch_floats_per_block(int nn, int nmat, int ckpt);
 cudaError_t tp2_blocks_per_sm(int nn, int nmat, Mode mode, bool philox, int *blocks);
 cudaError_t launch_tp2_any(const DevModel &m, Mode mode, const float *z, uint64_t seed, int64_t path0,
