@@ -188,14 +188,20 @@ int f32_family(const lmm_engine *e)
 }
 
 // Kernel family of an FP32 call: 5 (two threads per path, lmm_f32_tp2.cu)
-// for nn=160, nmat=120, every mode; otherwise f32_family. On GB300 at
-// 160/120 the thread pair runs 2.1x the warp-per-path rate; at 80/40 it ran
-// 13.4-15.5 ms against 11.7 ms for the thread-per-path kernel (4,194,304
-// paths), so it does not take that shape.
-int family_for(const lmm_engine *e, Mode)
+// for nn=160, nmat=120, every mode; 6 (one thread per path with the reverse
+// split over the rate halves, k_tps) for fused 80/40 calls (LMM_USE_TPS);
+// otherwise f32_family. On GB300 at 160/120 the thread pair runs 2.1x the
+// warp-per-path rate; at 80/40 it ran 13.4-15.5 ms against 11.7 ms for the
+// thread-per-path kernel (4,194,304 paths), so it does not take that shape.
+#ifndef LMM_USE_TPS
+#define LMM_USE_TPS 0
+#endif
+int family_for(const lmm_engine *e, Mode mode)
 {
     if (lmm::f32_tp2_supports(e->nn, e->nmat)) return 5;
-    return f32_family(e);
+    const int f = f32_family(e);
+    if (LMM_USE_TPS && f == 1 && mode == Mode::Fused) return 6;
+    return f;
 }
 
 // Paths one block takes per batch.
@@ -203,6 +209,7 @@ int batch_paths(const lmm_engine *e, int fam, Mode mode)
 {
     if (fam == 1) return lmm::tpp_block_threads(mode);
     if (fam == 5) return lmm::tp2_paths_per_block(e->nn);
+    if (fam == 6) return lmm::tps_block_threads();
     return lmm::wpp_block_threads() / 32;
 }
 
@@ -212,6 +219,7 @@ cudaError_t launch_f32_family(int fam, const lmm::DevModel &m, Mode mode, const 
 {
     if (fam == 1) return lmm::launch_tpp_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
     if (fam == 5) return lmm::launch_tp2_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
+    if (fam == 6) return lmm::launch_tps_any(m, z, seed, path0, philox, w, tape, s);
     return lmm::launch_wpp_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
 }
 
@@ -228,6 +236,7 @@ int blocks_per_sm(lmm_engine *e, int family, Mode mode, bool philox, int *out)
     if (family == 1) err = lmm::tpp_blocks_per_sm(mode, philox, &b);
     else if (family == 2) err = lmm::wpp_blocks_per_sm(e->nn, e->nmat, mode, philox, &b);
     else if (family == 5) err = lmm::tp2_blocks_per_sm(e->nn, e->nmat, mode, philox, &b);
+    else if (family == 6) err = lmm::tps_blocks_per_sm(philox, &b);
     else if (family == 3) err = lmm::f64_blocks_per_sm(false, &b);
     else err = lmm::f64_blocks_per_sm(true, &b);
     if (err != cudaSuccess) return cuda_fail(err, "occupancy query");
@@ -299,6 +308,17 @@ int wpp_scratch(lmm_engine *e, int64_t blocks, float **out)
     return LMM_OK;
 }
 
+// Scratch of the fused split-reverse kernel (k_tps) for a grid of `blocks`
+// blocks: per block the drift sums at the half boundary, the suffix sums
+// handed from the upper to the lower half, the lower half's parked rates and
+// the upper half's deltas.
+int tps_scratch(lmm_engine *e, int64_t blocks, float **out)
+{
+    LMM_TRY(e->wscratch.ensure(sizeof(float) * (size_t)blocks * lmm::tps_scratch_floats_per_block(e->nn, e->nmat)));
+    *out = e->wscratch.as<float>();
+    return LMM_OK;
+}
+
 // Scratch of the fused thread-pair kernel for a grid of `blocks` blocks: the
 // forward's drift sums at the half boundary and its rate checkpoints.
 int tp2_scratch(lmm_engine *e, int64_t blocks, float **out)
@@ -331,6 +351,7 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     LMM_TRY(plan(e, e->nscen, paths, per_batch, bps, nout, &w));
     if (fam == 2) LMM_TRY(wpp_scratch(e, w.grid, &tape));
     if (fam == 5 && mode == Mode::Fused) LMM_TRY(tp2_scratch(e, w.grid, &tape));
+    if (fam == 6) LMM_TRY(tps_scratch(e, w.grid, &tape));
     LMM_TRY(e->flag.ensure(sizeof(int)));
     LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
     mark(e, 0);
@@ -632,7 +653,7 @@ int lmm_engine_set_checkpoint_interval(lmm_engine *e, int32_t steps)
     if (fam == 0)
         return fail(LMM_ERR_UNSUPPORTED, "no FP32 kernel for nn=" + std::to_string(e->nn) +
                                              ", nmat=" + std::to_string(e->nmat));
-    if (fam == 1 && steps != 0)
+    if ((fam == 1 || fam == 6) && steps != 0)
         return fail(LMM_ERR_UNSUPPORTED, "the nn=80, nmat=40 kernel keeps every step's drift sums on chip and "
                                          "takes no rate checkpoints: only 0 is accepted");
     if (fam == 5 && steps % 2 != 0)
@@ -909,11 +930,12 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
     }
     LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)total_items * 2 * nout));
     float *wscr = nullptr;
-    if (fam == 2 || fam == 5) {
+    if (fam == 2 || fam == 5 || fam == 6) {
         int64_t most = 0;
         for (int c = 0; c < C; ++c) most = std::max(most, std::min<int64_t>(citems[c], (int64_t)e->sms * bps));
         // the pieces run one after another
-        LMM_TRY(fam == 2 ? wpp_scratch(e, most, &wscr) : tp2_scratch(e, most, &wscr));
+        LMM_TRY(fam == 2 ? wpp_scratch(e, most, &wscr)
+                         : (fam == 5 ? tp2_scratch(e, most, &wscr) : tps_scratch(e, most, &wscr)));
     }
     LMM_TRY(e->flag.ensure(sizeof(int)));
     if (!e->copy_stream) LMM_CK(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));

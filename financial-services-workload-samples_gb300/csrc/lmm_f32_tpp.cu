@@ -420,10 +420,9 @@ __device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float del
 // forward: rebuilding B[m-1] = B[m](1 + delta L) backwards from the last,
 // smallest factor would underflow FP32 on paths whose rates grow large.
 template <int NN, int NMAT, int B>
-__device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb)[NN], float vbar,
-                                               float V, float disc, const float *Bst, float *ILst,
-                                               unsigned long long mask, float delta,
-                                               const int *ost, const float *oKf, const float *oWf)
+__device__ __forceinline__ void payoff_adjoint_stage(float vbar, float disc, const float *Bst, float *ILst,
+                                                     unsigned long long mask, float delta, const int *ost,
+                                                     const float *oKf, const float *oWf)
 {
     constexpr int M = NN - NMAT;
     const float scale = -vbar * disc * delta;
@@ -448,6 +447,16 @@ __device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb
         ILst[m * B] = scale * Bb * Bm * t;
         Bb *= r;
     }
+}
+
+template <int NN, int NMAT, int B>
+__device__ __forceinline__ void payoff_adjoint(const float (&IL)[NN], float (&Pb)[NN], float vbar,
+                                               float V, float disc, const float *Bst, float *ILst,
+                                               unsigned long long mask, float delta,
+                                               const int *ost, const float *oKf, const float *oWf)
+{
+    constexpr int M = NN - NMAT;
+    payoff_adjoint_stage<NN, NMAT, B>(vbar, disc, Bst, ILst, mask, delta, ost, oKf, oWf);
 #pragma unroll
     for (int m = 0; m < M; ++m) Pb[NMAT + m] = ILst[m * B];
     const float vs = -vbar * V * delta;
@@ -717,6 +726,354 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     }  // units
 }
 
+// ---------------------------------------------------------------------------
+// k_tps: the fused kernel with the reverse sweep split over the two rate
+// halves, for more warps per SM.
+//
+// In k_tpp the reverse sweep holds all NN inverse rates and NN log-adjoints
+// in registers (232 per thread), which allows 8 warps per SM: two per
+// scheduler, too few to cover the cells' ex2 -> rcp dependency chains. The
+// forward needs only the NN rates. Here the reverse runs as two passes over
+// the halves of the rates, one after the other in the same thread:
+//   R1: rates H..NN-1 for every step, starting each step from the full drift
+//       sum (saved by the forward, shared memory) and an empty suffix sum;
+//       it leaves, per step, the suffix sum at rate H in the scratch;
+//   R2: rates 0..H-1 for every step, starting each step from the forward's
+//       drift sum at rate H-1 (scratch) and R1's suffix sum.
+// The lower half's terminal rates wait in the scratch during R1, the upper
+// half's deltas during R2, so at most H rates and H log-adjoints are live:
+// about 150 registers, 12 warps per SM (three per scheduler). The cells, the
+// step windows (G = 4 reverse steps per body, constants and vega partial sums
+// in rings), the payoff and the reductions are those of k_tpp; a vega row
+// takes read-modify-writes from both passes.
+// The scratch (per block of the wave, FP32, [row][B] so that a warp's 32
+// paths are contiguous): the drift sums at rate H-1 [NMAT], R1's suffix sums
+// at rate H [NMAT], the lower half's terminal inverse rates [H] and the upper
+// half's deltas [NN-H]. It is written and read back by the same thread within
+// one batch of B paths, and stays in L2 (about 37 MB per wave at NN = 80).
+// ---------------------------------------------------------------------------
+#ifndef LMM_TPS_BLOCK
+#define LMM_TPS_BLOCK 384
+#endif
+
+template <int NN, int NMAT>
+struct TpsLayout {
+    static constexpr int B = LMM_TPS_BLOCK;
+    static constexpr int NW = B / 32;
+    static constexpr int H = NN / 2;
+    static constexpr int M = NN - NMAT;
+    static constexpr int VPAD = 4;
+    static constexpr int NOUT = 1 + 2 * NN;
+    static constexpr int il0 = 0;                                    // float[NN]
+    static constexpr int ost = align16(il0 + 4 * NN);                // int[M+1]
+    static constexpr int okf = align16(ost + 4 * (M + 1));           // float[kMaxNopt]
+    static constexpr int owf = align16(okf + 4 * kMaxNopt);          // float[kMaxNopt]
+    static constexpr int okk = align16(owf + 4 * kMaxNopt);          // F2[kMaxNopt]
+    static constexpr int vt = align16(okk + 8 * kMaxNopt);           // float[NMAT][B] full drift sums
+    static constexpr int vg = vt + 4 * NMAT * B;                     // float[VPAD+NN][B] vega rows
+    static constexpr int acc = align16(vg + 4 * (VPAD + NN) * B);    // double[NW][2*NOUT]
+    static constexpr int bytes = acc + 8 * NW * 2 * NOUT;
+    // scratch rows per block
+    static constexpr int s_v = 0, s_s = NMAT, s_il = 2 * NMAT, s_d = 2 * NMAT + H, rows = 2 * NMAT + NN;
+    static_assert(NN % 2 == 0 && NMAT == H, "the upper half is the annuity rates");
+};
+
+// Forward steps n and n+1 as fwd_pair_window, also returning the drift sums
+// at rate CAP of both steps (the running sum after cell (n, CAP) and after
+// cell (n+1, CAP)); steps whose active rates all lie above CAP return their
+// starting value there.
+template <int NN, int CH, int P, int CAP>
+__device__ __forceinline__ void fwd_pair_window_cap(float (&IL)[NN], const float4 *kcn, float sqez0,
+                                                    float sqez1, float delta, int n, float &V0, float &V1,
+                                                    float &V0c, float &V1c)
+{
+    constexpr int R = 3 + P;
+    float4 C[R];
+    V0 = drift0(sqez0);
+    V1 = drift0(sqez1);
+    V0c = V0;
+    V1c = V1;
+    const int c0 = (n + 1) / CH;
+#pragma unroll
+    for (int c = 0; c * CH < NN; ++c) {
+        if (c >= c0) {
+            if (c == c0) {
+#pragma unroll
+                for (int j = c * CH - 2; j < c * CH + P; ++j)
+                    if (j >= 0 && j < NN) C[j % R] = kcn[j];
+            }
+#pragma unroll
+            for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
+                if (p + P < NN) C[(p + P) % R] = kcn[p + P];
+                if (p >= 1) fwd_cell(IL[p], V0, C[p % R], sqez0, delta);
+                if (p - 1 >= 1) fwd_cell(IL[p - 1], V1, C[(p + R - 2) % R], sqez1, delta);
+                if (p == CAP) V0c = V0;
+                if (p == CAP + 1) V1c = V1;
+            }
+        }
+    }
+    fwd_cell(IL[NN - 1], V1, C[(NN - 2) % R], sqez1, delta);
+}
+
+// Reverse steps n .. n-G+1 over one half of the rates, rates LO .. LO+H-1 held
+// in X[], Pb[] at local positions 0 .. H-1: rev_group_window on a block of
+// rates. st[0].kc and st[0].vg point at step n's constants and vega rows of
+// the block's local position 0. The upper half (LO > 0) is active in every
+// step (n < NMAT <= LO), so its body runs to the last position and flushes
+// the vega slots of positions 0 .. G-2, which hold its cells' sums; the lower
+// half (LO = 0) leaves the body as rev_group_window does.
+template <int H, int LO, int B, int G, int CH, int P>
+__device__ __forceinline__ void rev_half_window(float (&X)[H], float (&Pb)[H], RevStep (&st)[G], float delta,
+                                                int n)
+{
+    constexpr int JMAX = H + G - 2;
+    constexpr int W = 2 * G - 1 + P;
+    const float4 *kc = st[0].kc;
+    float *vg = st[0].vg;
+    float4 C[W];
+    float A[W];
+#pragma unroll
+    for (int j = H - P; j <= JMAX; ++j) {
+        C[j % W] = kc[j];
+        if (j >= H) A[j % W] = 0.0f;
+    }
+    const int imin = n - 2 * G + 3 - LO;     // lowest local position with an active cell
+#pragma unroll
+    for (int q = 0; q * CH < H + G - 1; ++q) {
+        const int top = H - 1 - q * CH;
+        if (LO == 0 && top < imin) return;
+#pragma unroll
+        for (int i = top; i > top - CH && i >= -(G - 1); --i) {
+            if (i - P >= (LO > 0 ? 0 : 1)) C[(i - P) % W] = kc[i - P];
+            if (i >= (LO > 0 ? 0 : 1)) A[i % W] = 0.0f;
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (i + g >= (LO > 0 ? 0 : 1) && i + g <= H - 1) {
+                    const int j = i + 2 * g;
+                    rev_cell<H>(X, Pb, st[g], i + g, C[j % W], A[j % W], delta);
+                }
+            }
+            const int jf = i + 2 * (G - 1);
+            if (jf >= (LO > 0 ? 0 : 1) && jf <= JMAX) vg[jf * B] += A[jf % W];
+        }
+    }
+    if (LO > 0) {
+#pragma unroll
+        for (int j = 0; j < G - 1; ++j) vg[j * B] += A[j % W];
+    }
+}
+
+template <int NN, int NMAT, bool PHILOX>
+__global__ void __launch_bounds__(LMM_TPS_BLOCK, 1)
+k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
+      float *__restrict__ scr, const __grid_constant__ TppConst<NN, NMAT> kp)
+{
+    using Lay = TpsLayout<NN, NMAT>;
+    constexpr int B = Lay::B, H = Lay::H, M = Lay::M, NOUT = Lay::NOUT, PAD = NMAT;
+    constexpr int G = LMM_TPP_SKEW, RCH = PHILOX ? LMM_TPP_RCHUNK_PHILOX : LMM_TPP_RCHUNK;
+    static_assert(NMAT % 4 == 0 && NMAT % G == 0, "normals in quads, reverse steps in groups");
+    static_assert(RCH - 1 <= Lay::VPAD, "the windows' spare vega rows lie inside the table");
+    extern __shared__ __align__(16) unsigned char smem[];
+    float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
+    int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
+    float *okf_s = reinterpret_cast<float *>(smem + Lay::okf);
+    float *owf_s = reinterpret_cast<float *>(smem + Lay::owf);
+    F2 *okk_s = reinterpret_cast<F2 *>(smem + Lay::okk);
+    float *vt_s = reinterpret_cast<float *>(smem + Lay::vt);
+    float *vg_s = reinterpret_cast<float *>(smem + Lay::vg);
+    double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i <= M; i += B) ost_s[i] = m.opt_start[i];
+    for (int i = tid; i < m.nopt; i += B) {
+        okf_s[i] = m.optKf[i];
+        owf_s[i] = m.optWf[i];
+        okk_s[i] = f2_from(m.optKd[i] * m.deltad);
+    }
+    double *acc = acc_s + warp * 2 * NOUT;
+    const float delta = m.delta, sqd = m.sqd;
+    const float4 *kc0 = kp.v + PAD;
+    float *vg0 = vg_s + Lay::VPAD * B + tid;
+    float *vt0 = vt_s + tid;
+    float *sc = scr + (size_t)blockIdx.x * Lay::rows * B + tid;    // sc[row * B]
+
+    const int units = m.nscen * w.items;
+    for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+        const int scen = unit / w.items, item = unit % w.items;
+        __syncthreads();          // the previous unit's reads of il0/acc are done
+        for (int i = tid; i < NN; i += B) il0_s[i] = m.invL0f[scen * NN + i];
+        for (int i = tid; i < Lay::NW * 2 * NOUT; i += B) acc_s[i] = 0.0;
+        __syncthreads();
+
+        const int64_t ibase = (int64_t)item * w.ppt * B;
+        for (int jb = 0; jb < w.ppt; ++jb) {
+            if (ibase + (int64_t)jb * B >= w.paths) break;          // block-uniform
+            const int64_t pl = ibase + (int64_t)jb * B + tid;
+            const bool active = pl < w.paths;
+            const int64_t pc = active ? pl : w.paths - 1;
+            const float *zp = PHILOX ? nullptr : z + pc * NMAT;
+            const uint64_t gpath = (uint64_t)(path0 + pc);
+
+            float disc = 1.0f, V, vs;
+            float Xu[H], Pu[H];       // upper half: inverse rates and log-adjoints
+            unsigned long long mask = 0ull;
+            {
+                // ---- forward over all NN rates (path_calc_b1 :34-82) ----
+                float IL[NN];
+#pragma unroll
+                for (int i = 0; i < NN; ++i) IL[i] = il0_s[i];
+                float4 zq, zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
+                for (int n = 0; n < NMAT; n += 2) {
+                    if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0)
+                        __syncthreads();
+                    if ((n & 3) == 0) {
+                        zq = zq_next;
+                        if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+                    }
+                    const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
+                    const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
+                    float V0, V1, V0c, V1c;
+                    fwd_pair_window_cap<NN, LMM_TPP_CHUNK, kPref<PHILOX>, H - 1>(IL, kc0 - (n + 1), sqez0, sqez1,
+                                                                                delta, n, V0, V1, V0c, V1c);
+                    vt0[n * B] = V0;
+                    vt0[(n + 1) * B] = V1;
+                    sc[(Lay::s_v + n) * B] = V0c;
+                    sc[(Lay::s_v + n + 1) * B] = V1c;
+                }
+                // ---- payoff (portfolio_b :133-171, :186-197) and the annuity adjoint ----
+                float *Bst = vg0;
+                float *ILst = vg0 + M * B;
+                V = payoff_forward<NN, NMAT, B>(IL, delta, ost_s, okk_s, owf_s, &disc, Bst, ILst, &mask);
+                payoff_adjoint_stage<NN, NMAT, B>(1.0f, disc, Bst, ILst, mask, delta, ost_s, okf_s, owf_s);
+#pragma unroll
+                for (int i = 0; i < H; ++i) {
+                    Xu[i] = IL[H + i];
+                    Pu[i] = ILst[i * B];
+                    sc[(Lay::s_il + i) * B] = IL[i];     // the lower half waits in the scratch
+                }
+                vs = -V * delta;
+            }
+#pragma unroll
+            for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+
+            // ---- R1: the upper half's reverse, every step ----
+            for (int n = NMAT - 1; n > 0; n -= G) {
+                if (LMM_TPP_SYNC) __syncthreads();
+                RevStep st[G];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    const int mm = n - g;
+                    st[g].sqez = 0.0f;
+                    st[g].V = vt0[mm * B];
+                    st[g].S = 0.0f;
+                    st[g].kc = kc0 - (mm + 1) + H;
+                    st[g].vg = vg0 + (H - mm - 1) * B;
+                }
+                rev_half_window<H, H, B, G, RCH, kPref<PHILOX>>(Xu, Pu, st, delta, n);
+#pragma unroll
+                for (int g = 0; g < G; ++g) sc[(Lay::s_s + n - g) * B] = st[g].S;
+            }
+#pragma unroll
+            for (int i = 0; i < H; ++i) sc[(Lay::s_d + i) * B] = active ? Pu[i] * il0_s[H + i] : 0.0f;
+
+            // ---- R2: the lower half's reverse ----
+            float Xl[H], Pl[H];
+#pragma unroll
+            for (int i = 0; i < H; ++i) {
+                Xl[i] = sc[(Lay::s_il + i) * B];
+                Pl[i] = vs * rcp_approx(Xl[i] + delta);
+            }
+            float nv[G], ns[G];       // the next group's restart sums, loaded a group ahead
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                nv[g] = sc[(Lay::s_v + NMAT - 1 - g) * B];
+                ns[g] = sc[(Lay::s_s + NMAT - 1 - g) * B];
+            }
+            for (int n = NMAT - 1; n > 0; n -= G) {
+                if (LMM_TPP_SYNC) __syncthreads();
+                RevStep st[G];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    const int mm = n - g;
+                    st[g].sqez = 0.0f;
+                    st[g].V = nv[g];
+                    st[g].S = ns[g];
+                    st[g].kc = kc0 - (mm + 1);
+                    st[g].vg = vg0 - (mm + 1) * B;
+                }
+                if (n - G > 0) {
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        nv[g] = sc[(Lay::s_v + n - G - g) * B];
+                        ns[g] = sc[(Lay::s_s + n - G - g) * B];
+                    }
+                }
+                rev_half_window<H, 0, B, G, RCH, kPref<PHILOX>>(Xl, Pl, st, delta, n);
+            }
+
+            // ---- cross-path reduction of this batch of B paths ----
+            {
+                const float v = active ? V : 0.0f;
+                const float s1 = warp_sum(v), s2 = warp_sum(v * v);
+                if (lane == 0) {
+                    acc[0] += (double)s1;
+                    acc[NOUT] += (double)s2;
+                }
+            }
+            float *vgw = vg_s + Lay::VPAD * B;
+            if (!active) {
+#pragma unroll
+                for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+            }
+            __syncwarp();
+            column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, 1 + NN);
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < H; ++i) {
+                vg0[i * B] = active ? Pl[i] * il0_s[i] : 0.0f;
+                vg0[(H + i) * B] = sc[(Lay::s_d + i) * B];
+            }
+            __syncwarp();
+            column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, 1);
+            __syncwarp();
+        }
+
+        __syncthreads();
+        for (int o = tid; o < 2 * NOUT; o += B) {
+            double s2 = 0.0;
+#pragma unroll
+            for (int q = 0; q < Lay::NW; ++q) s2 += acc_s[q * 2 * NOUT + o];
+            w.partial[(size_t)unit * 2 * NOUT + o] = s2;
+        }
+    }  // units
+}
+
+template <int NN, int NMAT, bool PHILOX>
+cudaError_t launch_tps(const DevModel &m, const float *z, uint64_t seed, int64_t path0, const Work &w,
+                       float *scr, cudaStream_t s)
+{
+    using Lay = TpsLayout<NN, NMAT>;
+    auto kern = k_tps<NN, NMAT, PHILOX>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
+    if (e != cudaSuccess) return e;
+    TppConst<NN, NMAT> kp;
+    for (int i = 0; i < NMAT + NN; ++i)
+        kp.v[i] = i < NMAT ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc_host[i - NMAT];
+    const unsigned grid = (unsigned)(w.grid > 0 ? w.grid : (int64_t)m.nscen * w.items);
+    kern<<<grid, Lay::B, Lay::bytes, s>>>(m, z, seed, path0, w, scr, kp);
+    return cudaGetLastError();
+}
+
+template <int NN, int NMAT, bool PHILOX>
+cudaError_t occ_tps(int *blocks)
+{
+    using Lay = TpsLayout<NN, NMAT>;
+    auto kern = k_tps<NN, NMAT, PHILOX>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, Lay::B, Lay::bytes);
+}
+
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
 cudaError_t launch_tpp(const DevModel &m, const float *z, uint64_t seed, int64_t path0,
                        const Work &w, float *tape, const double *vbar, cudaStream_t s)
@@ -746,6 +1103,22 @@ cudaError_t occ_tpp(int *blocks)
 }  // namespace
 
 bool f32_tpp_supports(int nn, int nmat) { return nn == 80 && nmat == 40; }
+
+int tps_block_threads() { return LMM_TPS_BLOCK; }
+
+size_t tps_scratch_floats_per_block(int nn, int nmat) { return (size_t)(2 * nmat + nn) * LMM_TPS_BLOCK; }
+
+cudaError_t tps_blocks_per_sm(bool philox, int *blocks)
+{
+    return philox ? occ_tps<80, 40, true>(blocks) : occ_tps<80, 40, false>(blocks);
+}
+
+cudaError_t launch_tps_any(const DevModel &m, const float *z, uint64_t seed, int64_t path0, bool philox,
+                           const Work &w, float *scratch, cudaStream_t s)
+{
+    return philox ? launch_tps<80, 40, true>(m, z, seed, path0, w, scratch, s)
+                  : launch_tps<80, 40, false>(m, z, seed, path0, w, scratch, s);
+}
 
 int tpp_block_threads(Mode mode)
 {

@@ -62,6 +62,14 @@ cudaError_t tpp_blocks_per_sm(Mode mode, bool philox, int *blocks);
 cudaError_t launch_tpp_any(const DevModel &m, Mode mode, const float *z, uint64_t seed,
                            int64_t path0, bool philox, const Work &w, float *tape,
                            const double *vbar, cudaStream_t s);
+// The fused 80/40 kernel with the reverse sweep split over the rate halves
+// (lmm_f32_tpp.cu, k_tps): 12 warps per SM, a per-block scratch of
+// tps_scratch_floats_per_block floats.
+int tps_block_threads();
+size_t tps_scratch_floats_per_block(int nn, int nmat);
+cudaError_t tps_blocks_per_sm(bool philox, int *blocks);
+cudaError_t launch_tps_any(const DevModel &m, const float *z, uint64_t seed, int64_t path0, bool philox,
+                           const Work &w, float *scratch, cudaStream_t s);
 // FP32 kernels with two threads per path (lmm_f32_tp2.cu): nn=160, nmat=120.
 // The forward/backward pair's tape: [nn][total] terminal inverse rates,
 // [nmat][total] full drift sums, [nmat][total] drift sums at rate nn/2 - 1.

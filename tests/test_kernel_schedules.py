@@ -247,3 +247,71 @@ def test_thread_per_path_reverse_windows(G, ch, p):
             step = n - g
             for i in range(step + 1, TPP_NN):
                 assert i - step - 1 in rows, (G, ch, n, step, i)
+
+
+def half_window(n, G, ch, p, H, lo, nn=TPP_NN):
+    """Replays rev_half_window (csrc/lmm_f32_tpp.cu, k_tps) for steps n..n-G+1
+    over rates lo..lo+H-1: returns the flushes as (row k, set of cells) and
+    the constant rows (as k) loaded. A cell is (step, rate)."""
+    W = 2 * G - 1 + p
+    jmax = H + G - 2
+    low = 0 if lo > 0 else 1
+    slots = {}
+    flushes, consts = [], set(range(H - p, jmax + 1))
+    for j in range(H, jmax + 1):
+        slots[j % W] = (j, set())
+    imin = n - 2 * G + 3 - lo
+    q = 0
+    while q * ch < H + G - 1:
+        top = H - 1 - q * ch
+        if lo == 0 and top < imin:
+            return flushes, {lo + j - n - 1 for j in consts}
+        i = top
+        while i > top - ch and i >= -(G - 1):
+            if i - p >= low:
+                consts.add(i - p)
+            if i >= low:
+                slots[i % W] = (i, set())
+            for g in range(G):
+                if low <= i + g <= H - 1:
+                    j = i + 2 * g
+                    sj, cells = slots[j % W]
+                    assert sj == j, (n, i, g, sj, j)          # the slot holds this j
+                    cells.add((n - g, lo + i + g))
+            jf = i + 2 * (G - 1)
+            if low <= jf <= jmax:
+                sj, cells = slots[jf % W]
+                assert sj == jf
+                flushes.append((lo + jf - n - 1, set(cells)))
+            i -= 1
+        q += 1
+    if lo > 0:
+        for j in range(G - 1):
+            sj, cells = slots[j % W]
+            assert sj == j
+            flushes.append((lo + j - n - 1, set(cells)))
+    return flushes, {lo + j - n - 1 for j in consts}
+
+
+@pytest.mark.parametrize("ch", [2, 4])
+def test_split_reverse_half_windows(ch):
+    """k_tps: the upper half (rates 40..79) and then the lower half (rates
+    0..39) over every group of four steps flush every active cell's vega
+    contribution exactly once, to the row k = rate - step - 1 of its own
+    step; rows with active cells lie in 0..NN-1, spare rows in -VPAD..-1, and
+    every constant row loaded in -NMAT..NN-1."""
+    G, p, H = 4, 1, TPP_NN // 2
+    seen = {}
+    for lo in (H, 0):
+        for n in range(TPP_NMAT - 1, 0, -G):
+            flushes, consts = half_window(n, G, ch, p, H, lo)
+            assert all(-TPP_PAD <= k <= TPP_NN - 1 for k in consts), (lo, n)
+            for k, cells in flushes:
+                assert -TPP_VPAD <= k <= TPP_NN - 1, (lo, n, k)
+                for step, rate in cells:
+                    if rate > step:                      # active cell
+                        assert k == rate - step - 1, (lo, n, step, rate, k)
+                        seen[(step, rate)] = seen.get((step, rate), 0) + 1
+    for step in range(TPP_NMAT):
+        for rate in range(step + 1, TPP_NN):
+            assert seen.get((step, rate)) == 1, (step, rate, seen.get((step, rate)))
