@@ -194,7 +194,7 @@ int f32_family(const lmm_engine *e)
 // warp-per-path rate; at 80/40 it ran 13.4-15.5 ms against 11.7 ms for the
 // thread-per-path kernel (4,194,304 paths), so it does not take that shape.
 #ifndef LMM_USE_TPS
-#define LMM_USE_TPS 0
+#define LMM_USE_TPS 1
 #endif
 int family_for(const lmm_engine *e, Mode mode)
 {

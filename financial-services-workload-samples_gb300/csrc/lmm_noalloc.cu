@@ -1,5 +1,6 @@
-// lmm_greeks_f32_device_noalloc: the fused FP32 value + Greeks launch for
-// callers that cannot allocate device memory.
+// lmm_greeks_f32_device_noalloc: a fused FP32 value + Greeks launch for
+// callers that cannot allocate device memory. It runs the one-pass fused
+// kernel (k_tpp), which needs no per-path scratch.
 //
 // Some callers cannot call cudaMalloc: code embedded in a host application
 // that owns every device allocation through its own pool, a plug-in whose

@@ -266,10 +266,12 @@ int lmm_mrg32k3a_normals_f32_device(uint32_t seed, int64_t first, int64_t count,
 /* No counterpart in the reference. Some callers cannot call cudaMalloc: a
  * library embedded in a host application that owns every device allocation
  * through its own pool, a plug-in whose process has locked or exhausted its
- * allocator, a loop that must never touch the allocator. This is the fused
- * FP32 value + Greeks launch of lmm_greeks_f32_device without an engine and
- * without any allocation (no cudaMalloc, no cudaFree, no allocating library
- * call). The caller passes the parameters, the device normals d_z and the
+ * allocator, a loop that must never touch the allocator. This is a fused
+ * FP32 value + Greeks launch like lmm_greeks_f32_device, without an engine
+ * and without any allocation (no cudaMalloc, no cudaFree, no allocating
+ * library call). It runs the one-pass kernel, which needs no per-path
+ * scratch; the engine's fused call runs the split-reverse kernel, and the
+ * two agree within the FP32 tolerance (same cells, rounded in another order). The caller passes the parameters, the device normals d_z and the
  * device outputs d_out/d_se (layout as above); everything else -- model
  * constants, per-block partial sums, the non-finite flag -- lives in one
  * static device array of LMM_NOALLOC_SCRATCH_BYTES that every GPU loading

@@ -65,10 +65,16 @@ def test_noalloc_matches_engine_on_two_calls_in_a_row(nscen):
         g = out.cpu().numpy().reshape(nscen, cfg.nout)
         g_se = se.cpu().numpy().reshape(nscen, cfg.nout)
         for s in range(nscen):
-            # same kernel and arithmetic; only the FP64 summation grouping may differ
+            # the engine's fused call runs the split-reverse kernel, this call
+            # the one-pass kernel: the same cells, rounded in another order,
+            # so they agree within the FP32 rule of the parity tests
             assert _scaled_err(g[s], r[s], cfg.nn) <= 1e-4
-            np.testing.assert_allclose(g[s], r[s], rtol=1e-9, atol=1e-12 * np.abs(r[s]).max())
-            np.testing.assert_allclose(g_se[s], r_se[s], rtol=1e-6)
+            np.testing.assert_allclose(g_se[s], r_se[s], rtol=1e-4)
+        if call == 1:
+            # the second call sees the first call's leftovers in the shared
+            # array and still returns the same bits
+            np.testing.assert_array_equal(outs[2].cpu().numpy(), outs[0].cpu().numpy())
+            np.testing.assert_array_equal(outs[3].cpu().numpy(), outs[1].cpu().numpy())
 
 
 def test_noalloc_limits_are_errors():
