@@ -373,8 +373,9 @@ def run_ours(args):
         phases = {"forward_ms": fw, "backward_ms": bw, "fused_ms": statistics.median(kern_ms),
                   "tape_bytes": 4 * (cfg.nn + nmat) * n,
                   "note": "forward = Euler steps + payoff + tape write (terminal rates, per-step drift "
-                          "sums); backward = tape read + payoff adjoint + reverse sweep; the fused "
-                          "kernel keeps both in registers and shared memory"}
+                          "sums); backward = tape read + payoff adjoint + reverse sweep (the pair runs "
+                          "the one-pass k_tpp kernels); the fused call keeps its state on chip, the "
+                          "idle rate half in an L2 scratch"}
 
     # ---- the MRG32k3a/AS241 normal stream (the reference's generator family):
     # the workload's normals generated on the device vs the oracle on one core
@@ -476,7 +477,7 @@ def run_ours(args):
                 kms = sorted(kt)[1]
                 others[c.name] = {"paths_per_s": c.nscen * c.paths / (kms * 1e-3), "ms": kms,
                                   "nn": c.nn, "nmat": c.nmat, "scenarios": c.nscen, "normals": mode,
-                                  "kernel": "k_tpp (thread per path)" if c.nn == 80 else
+                                  "kernel": "k_tps (thread per path, reverse split over the rate halves)" if c.nn == 80 else
                                   "k_tp2 (two threads per path in alternating blocks of 40 rates; reverse "
                                   "rebuilt from each block's top drift sums, rates saved every 8 steps)"}
                 del zw
@@ -493,7 +494,7 @@ def run_ours(args):
                 prof = json.load(f)
             traffic = prof.get("dram_bytes_per_launch")
         achieved = ops / (kms * 1e-3) / 1e12
-        roof = {"bound": "fp32", "kernel": "k_tpp<80,40,hbm,fused>", "achieved": achieved,
+        roof = {"bound": "fp32", "kernel": "k_tps<80,40,hbm>", "achieved": achieved,
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "peak_source": "measured live: FFMA-chain kernel lmm_fp32_peak_tflops (MEASURED_PEAKS.json "
                                "has no FP32 SIMT figure)",
