@@ -755,6 +755,11 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 #ifndef LMM_TPS_BLOCK
 #define LMM_TPS_BLOCK 384
 #endif
+// Barriers in k_tps's step loops (0: none; they keep the warps of a block on
+// the same stretch of code; every array the loops touch is per thread).
+#ifndef LMM_TPS_SYNC
+#define LMM_TPS_SYNC LMM_TPP_SYNC
+#endif
 
 template <int NN, int NMAT>
 struct TpsLayout {
@@ -864,7 +869,7 @@ __device__ __forceinline__ void rev_half_window(float (&X)[H], float (&Pb)[H], R
 }
 
 template <int NN, int NMAT, bool PHILOX>
-__global__ void __launch_bounds__(LMM_TPS_BLOCK, 1)
+__global__ void __launch_bounds__(LMM_TPS_BLOCK, 384 / LMM_TPS_BLOCK)
 k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
       float *__restrict__ scr, const __grid_constant__ TppConst<NN, NMAT> kp)
 {
@@ -924,7 +929,7 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 for (int i = 0; i < NN; ++i) IL[i] = il0_s[i];
                 float4 zq, zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
                 for (int n = 0; n < NMAT; n += 2) {
-                    if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0)
+                    if (LMM_TPS_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0)
                         __syncthreads();
                     if ((n & 3) == 0) {
                         zq = zq_next;
@@ -958,7 +963,7 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 
             // ---- R1: the upper half's reverse, every step ----
             for (int n = NMAT - 1; n > 0; n -= G) {
-                if (LMM_TPP_SYNC) __syncthreads();
+                if (LMM_TPS_SYNC) __syncthreads();
                 RevStep st[G];
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
@@ -990,7 +995,7 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 ns[g] = sc[(Lay::s_s + NMAT - 1 - g) * B];
             }
             for (int n = NMAT - 1; n > 0; n -= G) {
-                if (LMM_TPP_SYNC) __syncthreads();
+                if (LMM_TPS_SYNC) __syncthreads();
                 RevStep st[G];
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
