@@ -760,6 +760,11 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 #ifndef LMM_TPS_SYNC
 #define LMM_TPS_SYNC LMM_TPP_SYNC
 #endif
+// 1: k_tps reads the per-maturity constants from the kernel-parameter bank;
+// 0: from shared memory.
+#ifndef LMM_TPS_KCPARAM
+#define LMM_TPS_KCPARAM 1
+#endif
 
 template <int NN, int NMAT>
 struct TpsLayout {
@@ -776,7 +781,8 @@ struct TpsLayout {
     static constexpr int okk = align16(owf + 4 * kMaxNopt);          // F2[kMaxNopt]
     static constexpr int vt = align16(okk + 8 * kMaxNopt);           // float[NMAT][B] full drift sums
     static constexpr int vg = vt + 4 * NMAT * B;                     // float[VPAD+NN][B] vega rows
-    static constexpr int acc = align16(vg + 4 * (VPAD + NN) * B);    // double[NW][2*NOUT]
+    static constexpr int kc = align16(vg + 4 * (VPAD + NN) * B);     // float4[NMAT+NN] (!LMM_TPS_KCPARAM)
+    static constexpr int acc = align16(kc + (LMM_TPS_KCPARAM ? 0 : 16 * (NMAT + NN)));   // double[NW][2*NOUT]
     static constexpr int bytes = acc + 8 * NW * 2 * NOUT;
     // scratch rows per block
     static constexpr int s_v = 0, s_s = NMAT, s_il = 2 * NMAT, s_d = 2 * NMAT + H, rows = 2 * NMAT + NN;
@@ -897,7 +903,11 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     }
     double *acc = acc_s + warp * 2 * NOUT;
     const float delta = m.delta, sqd = m.sqd;
-    const float4 *kc0 = kp.v + PAD;
+    float4 *kc_s = reinterpret_cast<float4 *>(smem + Lay::kc);
+    if (!LMM_TPS_KCPARAM) {
+        for (int i = tid; i < PAD + NN; i += B) kc_s[i] = kp.v[i];
+    }
+    const float4 *kc0 = (LMM_TPS_KCPARAM ? kp.v : kc_s) + PAD;
     float *vg0 = vg_s + Lay::VPAD * B + tid;
     float *vt0 = vt_s + tid;
     float *sc = scr + (size_t)blockIdx.x * Lay::rows * B + tid;    // sc[row * B]
