@@ -196,9 +196,15 @@ int f32_family(const lmm_engine *e)
 #ifndef LMM_USE_TPS
 #define LMM_USE_TPS 1
 #endif
+// 7 (one thread per path, the reverse in passes over blocks of 40 rates,
+// k_tpq) for fused 160/120 calls (LMM_USE_TPQ); the pair keeps family 5.
+#ifndef LMM_USE_TPQ
+#define LMM_USE_TPQ 0
+#endif
 int family_for(const lmm_engine *e, Mode mode)
 {
-    if (lmm::f32_tp2_supports(e->nn, e->nmat)) return 5;
+    if (lmm::f32_tp2_supports(e->nn, e->nmat))
+        return LMM_USE_TPQ && mode == Mode::Fused && lmm::f32_tpq_supports(e->nn, e->nmat) ? 7 : 5;
     const int f = f32_family(e);
     if (LMM_USE_TPS && f == 1 && mode == Mode::Fused) return 6;
     return f;
@@ -210,6 +216,7 @@ int batch_paths(const lmm_engine *e, int fam, Mode mode)
     if (fam == 1) return lmm::tpp_block_threads(mode);
     if (fam == 5) return lmm::tp2_paths_per_block(e->nn);
     if (fam == 6) return lmm::tps_block_threads();
+    if (fam == 7) return lmm::tpq_block_threads();
     return lmm::wpp_block_threads() / 32;
 }
 
@@ -220,6 +227,7 @@ cudaError_t launch_f32_family(int fam, const lmm::DevModel &m, Mode mode, const 
     if (fam == 1) return lmm::launch_tpp_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
     if (fam == 5) return lmm::launch_tp2_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
     if (fam == 6) return lmm::launch_tps_any(m, z, seed, path0, philox, w, tape, s);
+    if (fam == 7) return lmm::launch_tpq_any(m, z, seed, path0, philox, w, tape, s);
     return lmm::launch_wpp_any(m, mode, z, seed, path0, philox, w, tape, vbar, s);
 }
 
@@ -237,6 +245,7 @@ int blocks_per_sm(lmm_engine *e, int family, Mode mode, bool philox, int *out)
     else if (family == 2) err = lmm::wpp_blocks_per_sm(e->nn, e->nmat, mode, philox, &b);
     else if (family == 5) err = lmm::tp2_blocks_per_sm(e->nn, e->nmat, mode, philox, &b);
     else if (family == 6) err = lmm::tps_blocks_per_sm(philox, &b);
+    else if (family == 7) err = lmm::tpq_blocks_per_sm(philox, &b);
     else if (family == 3) err = lmm::f64_blocks_per_sm(false, &b);
     else err = lmm::f64_blocks_per_sm(true, &b);
     if (err != cudaSuccess) return cuda_fail(err, "occupancy query");
@@ -319,6 +328,17 @@ int tps_scratch(lmm_engine *e, int64_t blocks, float **out)
     return LMM_OK;
 }
 
+// Scratch of the fused long-tenor block-pass kernel (k_tpq) for a grid of
+// `blocks` blocks: block-top drift sums, block-bottom suffix sums, parked
+// rates and deltas, and the rate checkpoints of the engine's interval.
+int tpq_scratch(lmm_engine *e, int64_t blocks, float **out)
+{
+    LMM_TRY(e->wscratch.ensure(sizeof(float) * (size_t)blocks *
+                               lmm::tpq_scratch_floats_per_block(e->nn, e->nmat, e->dm.ckpt)));
+    *out = e->wscratch.as<float>();
+    return LMM_OK;
+}
+
 // Scratch of the fused thread-pair kernel for a grid of `blocks` blocks: the
 // forward's drift sums at the half boundary and its rate checkpoints.
 int tp2_scratch(lmm_engine *e, int64_t blocks, float **out)
@@ -352,6 +372,7 @@ int run_f32(lmm_engine *e, Mode mode, const float *d_z, uint64_t seed, int64_t p
     if (fam == 2) LMM_TRY(wpp_scratch(e, w.grid, &tape));
     if (fam == 5 && mode == Mode::Fused) LMM_TRY(tp2_scratch(e, w.grid, &tape));
     if (fam == 6) LMM_TRY(tps_scratch(e, w.grid, &tape));
+    if (fam == 7) LMM_TRY(tpq_scratch(e, w.grid, &tape));
     LMM_TRY(e->flag.ensure(sizeof(int)));
     LMM_CK(cudaMemsetAsync(e->flag.p, 0, sizeof(int), e->stream));
     mark(e, 0);
@@ -659,6 +680,9 @@ int lmm_engine_set_checkpoint_interval(lmm_engine *e, int32_t steps)
     if (fam == 5 && steps % 2 != 0)
         return fail(LMM_ERR_UNSUPPORTED, "the nn=160, nmat=120 kernel runs its steps in pairs: the interval "
                                          "must be even");
+    if (fam == 7 && steps % 4 != 0)
+        return fail(LMM_ERR_UNSUPPORTED, "the nn=160, nmat=120 kernel restores checkpoints between groups of "
+                                         "four reverse steps: the interval must be a multiple of 4");
     e->dm.ckpt = steps;
     return LMM_OK;
 }
@@ -930,12 +954,13 @@ int run_f32_host_pipelined(lmm_engine *e, const float *z, int64_t paths)
     }
     LMM_TRY(e->partial.ensure(sizeof(double) * (size_t)total_items * 2 * nout));
     float *wscr = nullptr;
-    if (fam == 2 || fam == 5 || fam == 6) {
+    if (fam == 2 || fam == 5 || fam == 6 || fam == 7) {
         int64_t most = 0;
         for (int c = 0; c < C; ++c) most = std::max(most, std::min<int64_t>(citems[c], (int64_t)e->sms * bps));
         // the pieces run one after another
         LMM_TRY(fam == 2 ? wpp_scratch(e, most, &wscr)
-                         : (fam == 5 ? tp2_scratch(e, most, &wscr) : tps_scratch(e, most, &wscr)));
+                         : fam == 5 ? tp2_scratch(e, most, &wscr)
+                                    : fam == 6 ? tps_scratch(e, most, &wscr) : tpq_scratch(e, most, &wscr));
     }
     LMM_TRY(e->flag.ensure(sizeof(int)));
     if (!e->copy_stream) LMM_CK(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));

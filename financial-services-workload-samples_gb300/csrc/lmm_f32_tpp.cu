@@ -1089,6 +1089,372 @@ cudaError_t occ_tps(int *blocks)
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, Lay::B, Lay::bytes);
 }
 
+// ---------------------------------------------------------------------------
+// k_tpq: the fused long-tenor call (NN = 160, NMAT = 120) with one thread per
+// path, the reverse sweep in passes over blocks of 40 rates.
+//
+// The forward holds all NN inverse rates in registers (about 200 registers:
+// 8 warps, 256 paths per SM) and saves, per step, the drift sum at the top
+// rate of every block and the rates every ck steps (ck = DevModel::ckpt, a
+// multiple of 4). The reverse then runs the blocks one after another from the
+// top, in one thread: block b (rates 40b .. 40b+39) for every group of four
+// steps with an active cell in it, each step starting from the forward's
+// drift sum at the block's top rate and from the suffix sum the block above
+// left at its bottom; the rates above a checkpoint time are taken back from
+// the checkpoint at group boundaries. At most 40 rates and 40 log-adjoints
+// are live in the reverse, the other blocks wait in a per-block scratch, and
+// one copy of the 40-position reverse body serves every block (the block's
+// offset is a runtime value). Against two threads per path (k_tp2) there is
+// no pair to balance and no barrier per round: the same cells run with the
+// occupancy and schedule of the 80/40 kernels.
+// Scratch per block of the wave, rows of B floats (one per thread):
+// [Q][NMAT] block-top drift sums, [Q-1][NMAT] block-bottom suffix sums,
+// [NN-H] parked inverse rates of the lower blocks, [NN-H] deltas of the upper
+// blocks, [NCK][NN] rate checkpoints.
+// ---------------------------------------------------------------------------
+#ifndef LMM_TPQ_BLOCK
+#define LMM_TPQ_BLOCK 256
+#endif
+
+template <int NN, int NMAT>
+struct TpqLayout {
+    static constexpr int B = LMM_TPQ_BLOCK;
+    static constexpr int NW = B / 32;
+    static constexpr int H = 40;
+    static constexpr int Q = NN / H;
+    static constexpr int M = NN - NMAT;
+    static constexpr int VPAD = 4;
+    static constexpr int NOUT = 1 + 2 * NN;
+    static constexpr int il0 = 0;                                    // float[NN]
+    static constexpr int ost = align16(il0 + 4 * NN);                // int[M+1]
+    static constexpr int okf = align16(ost + 4 * (M + 1));           // float[kMaxNopt]
+    static constexpr int owf = align16(okf + 4 * kMaxNopt);          // float[kMaxNopt]
+    static constexpr int okk = align16(owf + 4 * kMaxNopt);          // F2[kMaxNopt]
+    static constexpr int vg = align16(okk + 8 * kMaxNopt);           // float[VPAD+NN][B] vega rows
+    static constexpr int acc = align16(vg + 4 * (VPAD + NN) * B);    // double[NW][2*NOUT]
+    static constexpr int bytes = acc + 8 * NW * 2 * NOUT;
+    static constexpr int s_vt = 0, s_sb = Q * NMAT, s_il = s_sb + (Q - 1) * NMAT, s_d = s_il + NN - H,
+                         s_ck = s_d + NN - H;
+    static_assert(NN % H == 0 && M == H && H % 4 == 0, "the top block is the annuity rates");
+};
+
+// Forward steps n and n+1 as fwd_pair_window, also returning the drift sums
+// of both steps at the top rate of every H-rate block but the last.
+template <int NN, int H, int CH, int P>
+__device__ __forceinline__ void fwd_pair_window_caps(float (&IL)[NN], const float4 *kcn, float sqez0,
+                                                     float sqez1, float delta, int n, float &V0, float &V1,
+                                                     float (&V0c)[NN / H - 1], float (&V1c)[NN / H - 1])
+{
+    constexpr int R = 3 + P;
+    float4 C[R];
+    V0 = drift0(sqez0);
+    V1 = drift0(sqez1);
+#pragma unroll
+    for (int b = 0; b < NN / H - 1; ++b) {
+        V0c[b] = V0;
+        V1c[b] = V1;
+    }
+    const int c0 = (n + 1) / CH;
+#pragma unroll
+    for (int c = 0; c * CH < NN; ++c) {
+        if (c >= c0) {
+            if (c == c0) {
+#pragma unroll
+                for (int j = c * CH - 2; j < c * CH + P; ++j)
+                    if (j >= 0 && j < NN) C[j % R] = kcn[j];
+            }
+#pragma unroll
+            for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
+                if (p + P < NN) C[(p + P) % R] = kcn[p + P];
+                if (p >= 1) fwd_cell(IL[p], V0, C[p % R], sqez0, delta);
+                if (p - 1 >= 1) fwd_cell(IL[p - 1], V1, C[(p + R - 2) % R], sqez1, delta);
+                if (p % H == H - 1 && p < NN - 1) V0c[p / H] = V0;
+                if (p >= 1 && (p - 1) % H == H - 1 && p - 1 < NN - 1) V1c[(p - 1) / H] = V1;
+            }
+        }
+    }
+    fwd_cell(IL[NN - 1], V1, C[(NN - 2) % R], sqez1, delta);
+}
+
+// Reverse steps n .. n-G+1 over the block of H rates LO .. LO+H-1 (X[], Pb[]
+// at local positions 0 .. H-1; LO a runtime multiple of G): rev_group_window
+// on a block. st[0].kc and st[0].vg point at step n's constants and vega rows
+// of the block's local position 0. When every step of the group is active at
+// the block's bottom rate (LO > n) the body runs to its last position and
+// flushes the vega slots of positions 0 .. G-2 (they hold active cells);
+// otherwise it is left at the first chunk wholly below the lowest active
+// position, as rev_group_window, and the slots still open hold no-op cells
+// of spare rows.
+template <int H, int B, int G, int CH, int P>
+__device__ __forceinline__ void rev_block_window(float (&X)[H], float (&Pb)[H], RevStep (&st)[G], float delta,
+                                                 int n, int LO)
+{
+    constexpr int JMAX = H + G - 2;
+    constexpr int W = 2 * G - 1 + P;
+    const float4 *kc = st[0].kc;
+    float *vg = st[0].vg;
+    float4 C[W];
+    float A[W];
+#pragma unroll
+    for (int j = H - P; j <= JMAX; ++j) {
+        C[j % W] = kc[j];
+        if (j >= H) A[j % W] = 0.0f;
+    }
+    const bool full = LO > n;
+    const int imin = n - 2 * G + 3 - LO;     // lowest local position with an active cell
+#pragma unroll
+    for (int q = 0; q * CH < H + G - 1; ++q) {
+        const int top = H - 1 - q * CH;
+        if (!full && top < imin) return;
+#pragma unroll
+        for (int i = top; i > top - CH && i >= -(G - 1); --i) {
+            if (i - P >= 0) C[(i - P) % W] = kc[i - P];
+            if (i >= 0) A[i % W] = 0.0f;
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (i + g >= 0 && i + g <= H - 1) {
+                    const int j = i + 2 * g;
+                    rev_cell<H>(X, Pb, st[g], i + g, C[j % W], A[j % W], delta);
+                }
+            }
+            const int jf = i + 2 * (G - 1);
+            if (jf >= 0 && jf <= JMAX) vg[jf * B] += A[jf % W];
+        }
+    }
+    if (full) {
+#pragma unroll
+        for (int j = 0; j < G - 1; ++j) vg[j * B] += A[j % W];
+    }
+}
+
+template <int NN, int NMAT, bool PHILOX>
+__global__ void __launch_bounds__(LMM_TPQ_BLOCK, 1)
+k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path0, const Work w,
+      float *__restrict__ scr, const __grid_constant__ TppConst<NN, NMAT> kp)
+{
+    using Lay = TpqLayout<NN, NMAT>;
+    constexpr int B = Lay::B, H = Lay::H, Q = Lay::Q, M = Lay::M, NOUT = Lay::NOUT, PAD = NMAT;
+    constexpr int G = LMM_TPP_SKEW, RCH = PHILOX ? LMM_TPP_RCHUNK_PHILOX : LMM_TPP_RCHUNK;
+    static_assert(NMAT % 4 == 0 && NMAT % G == 0 && H % G == 0, "normals in quads, reverse steps in groups");
+    static_assert(RCH - 1 <= Lay::VPAD, "the windows' spare vega rows lie inside the table");
+    extern __shared__ __align__(16) unsigned char smem[];
+    float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
+    int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
+    float *okf_s = reinterpret_cast<float *>(smem + Lay::okf);
+    float *owf_s = reinterpret_cast<float *>(smem + Lay::owf);
+    F2 *okk_s = reinterpret_cast<F2 *>(smem + Lay::okk);
+    float *vg_s = reinterpret_cast<float *>(smem + Lay::vg);
+    double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i <= M; i += B) ost_s[i] = m.opt_start[i];
+    for (int i = tid; i < m.nopt; i += B) {
+        okf_s[i] = m.optKf[i];
+        owf_s[i] = m.optWf[i];
+        okk_s[i] = f2_from(m.optKd[i] * m.deltad);
+    }
+    double *acc = acc_s + warp * 2 * NOUT;
+    const float delta = m.delta, sqd = m.sqd;
+    const float4 *kc0 = kp.v + PAD;
+    float *vg0 = vg_s + Lay::VPAD * B + tid;
+    const int ck = m.ckpt;
+    const int nck = ck > 0 ? (NMAT - 1) / ck : 0;
+    const int ckd = ck > 0 ? ck : 1;
+    const int64_t rows = Lay::s_ck + (int64_t)nck * NN;
+    float *sc = scr + (size_t)blockIdx.x * rows * B + tid;          // sc[row * B]
+    float *ckp = sc + (size_t)Lay::s_ck * B;                         // checkpoint c, rate i: ckp[(c*NN + i)*B]
+
+    const int units = m.nscen * w.items;
+    for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+        const int scen = unit / w.items, item = unit % w.items;
+        __syncthreads();          // the previous unit's reads of il0/acc are done
+        for (int i = tid; i < NN; i += B) il0_s[i] = m.invL0f[scen * NN + i];
+        for (int i = tid; i < Lay::NW * 2 * NOUT; i += B) acc_s[i] = 0.0;
+        __syncthreads();
+
+        const int64_t ibase = (int64_t)item * w.ppt * B;
+        for (int jb = 0; jb < w.ppt; ++jb) {
+            if (ibase + (int64_t)jb * B >= w.paths) break;          // block-uniform
+            const int64_t pl = ibase + (int64_t)jb * B + tid;
+            const bool active = pl < w.paths;
+            const int64_t pc = active ? pl : w.paths - 1;
+            const float *zp = PHILOX ? nullptr : z + pc * NMAT;
+            const uint64_t gpath = (uint64_t)(path0 + pc);
+
+            float disc = 1.0f, V, vs;
+            float X[H], Pb[H];        // the block in the reverse: inverse rates, log-adjoints
+            unsigned long long mask = 0ull;
+            {
+                // ---- forward over all NN rates (path_calc_b1 :34-82) ----
+                float IL[NN];
+#pragma unroll
+                for (int i = 0; i < NN; ++i) IL[i] = il0_s[i];
+                float4 zq, zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
+                for (int n = 0; n < NMAT; n += 2) {
+                    if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0)
+                        __syncthreads();
+                    if ((n & 3) == 0) {
+                        zq = zq_next;
+                        if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+                    }
+                    const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
+                    const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
+                    float V0, V1, V0c[Q - 1], V1c[Q - 1];
+                    fwd_pair_window_caps<NN, H, LMM_TPP_CHUNK, kPref<PHILOX>>(IL, kc0 - (n + 1), sqez0, sqez1, delta,
+                                                                             n, V0, V1, V0c, V1c);
+#pragma unroll
+                    for (int b = 0; b < Q - 1; ++b) {
+                        sc[(Lay::s_vt + b * NMAT + n) * B] = V0c[b];
+                        sc[(Lay::s_vt + b * NMAT + n + 1) * B] = V1c[b];
+                    }
+                    sc[(Lay::s_vt + (Q - 1) * NMAT + n) * B] = V0;
+                    sc[(Lay::s_vt + (Q - 1) * NMAT + n + 1) * B] = V1;
+                    if (nck > 0 && (n + 2) % ckd == 0 && n + 2 < NMAT) {
+                        // rates i <= n+2 are final from here on: only the others are saved
+                        const int c = (n + 2) / ckd - 1;
+#pragma unroll
+                        for (int i = 0; i < NN; ++i)
+                            if (i > n + 2) ckp[(c * NN + i) * B] = IL[i];
+                    }
+                }
+                // ---- payoff (portfolio_b :133-171, :186-197) and the annuity adjoint ----
+                float *Bst = vg0;
+                float *ILst = vg0 + M * B;
+                V = payoff_forward<NN, NMAT, B>(IL, delta, ost_s, okk_s, owf_s, &disc, Bst, ILst, &mask);
+                payoff_adjoint_stage<NN, NMAT, B>(1.0f, disc, Bst, ILst, mask, delta, ost_s, okf_s, owf_s);
+#pragma unroll
+                for (int i = 0; i < H; ++i) {
+                    X[i] = IL[NN - H + i];
+                    Pb[i] = ILst[i * B];
+                }
+#pragma unroll
+                for (int i = 0; i < NN - H; ++i) sc[(Lay::s_il + i) * B] = IL[i];
+                vs = -V * delta;
+            }
+#pragma unroll
+            for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+
+            // ---- reverse: the blocks from the top, each over its groups of steps ----
+            for (int b = Q - 1; b >= 0; --b) {
+                const int LO = b * H;
+                if (b < Q - 1) {
+#pragma unroll
+                    for (int i = 0; i < H; ++i) {
+                        X[i] = sc[(Lay::s_il + LO + i) * B];
+                        Pb[i] = vs * rcp_approx(X[i] + delta);
+                    }
+                }
+                // the block's first group with an active cell (its top rate above the group's lowest step)
+                int n0 = NMAT - 1;
+                while (LO + H - 1 <= n0 - G + 1) n0 -= G;
+                float nv[G], ns[G];   // the next group's restart sums, loaded a group ahead
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    nv[g] = sc[(Lay::s_vt + b * NMAT + n0 - g) * B];
+                    ns[g] = b < Q - 1 ? sc[(Lay::s_sb + b * NMAT + n0 - g) * B] : 0.0f;
+                }
+                for (int n = n0; n > 0; n -= G) {
+                    if (LMM_TPP_SYNC) __syncthreads();
+                    RevStep st[G];
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        const int mm = n - g;
+                        st[g].sqez = 0.0f;
+                        st[g].V = nv[g];
+                        st[g].S = ns[g];
+                        st[g].kc = kc0 - (mm + 1) + LO;
+                        st[g].vg = vg0 + (LO - mm - 1) * B;
+                    }
+                    if (n - G > 0) {
+#pragma unroll
+                        for (int g = 0; g < G; ++g) {
+                            nv[g] = sc[(Lay::s_vt + b * NMAT + n - G - g) * B];
+                            ns[g] = b < Q - 1 ? sc[(Lay::s_sb + b * NMAT + n - G - g) * B] : 0.0f;
+                        }
+                    }
+                    rev_block_window<H, B, G, RCH, kPref<PHILOX>>(X, Pb, st, delta, n, LO);
+                    if (b > 0) {
+#pragma unroll
+                        for (int g = 0; g < G; ++g) sc[(Lay::s_sb + (b - 1) * NMAT + n - g) * B] = st[g].S;
+                    }
+                    const int t = n - G + 1;          // the time the group leaves the rates at
+                    if (nck > 0 && t % ckd == 0 && t >= ck) {
+                        // the reverse of steps >= t leaves rates i <= t untouched
+                        const int c = t / ckd - 1;
+#pragma unroll
+                        for (int i = 0; i < H; ++i)
+                            if (LO + i > t) X[i] = ckp[(c * NN + LO + i) * B];
+                    }
+                }
+                if (b > 0) {
+#pragma unroll
+                    for (int i = 0; i < H; ++i)
+                        sc[(Lay::s_d + LO - H + i) * B] = active ? Pb[i] * il0_s[LO + i] : 0.0f;
+                }
+            }
+
+            // ---- cross-path reduction of this batch of B paths ----
+            {
+                const float v = active ? V : 0.0f;
+                const float s1 = warp_sum(v), s2 = warp_sum(v * v);
+                if (lane == 0) {
+                    acc[0] += (double)s1;
+                    acc[NOUT] += (double)s2;
+                }
+            }
+            float *vgw = vg_s + Lay::VPAD * B;
+            if (!active) {
+#pragma unroll
+                for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
+            }
+            __syncwarp();
+            column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, 1 + NN);
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < H; ++i) vg0[i * B] = active ? Pb[i] * il0_s[i] : 0.0f;
+#pragma unroll
+            for (int i = 0; i < NN - H; ++i) vg0[(H + i) * B] = sc[(Lay::s_d + i) * B];
+            __syncwarp();
+            column_reduce<NN, B>(vgw, warp, lane, acc, NOUT, 1);
+            __syncwarp();
+        }
+
+        __syncthreads();
+        for (int o = tid; o < 2 * NOUT; o += B) {
+            double s2 = 0.0;
+#pragma unroll
+            for (int q = 0; q < Lay::NW; ++q) s2 += acc_s[q * 2 * NOUT + o];
+            w.partial[(size_t)unit * 2 * NOUT + o] = s2;
+        }
+    }  // units
+}
+
+template <int NN, int NMAT, bool PHILOX>
+cudaError_t launch_tpq(const DevModel &m, const float *z, uint64_t seed, int64_t path0, const Work &w,
+                       float *scr, cudaStream_t s)
+{
+    using Lay = TpqLayout<NN, NMAT>;
+    auto kern = k_tpq<NN, NMAT, PHILOX>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
+    if (e != cudaSuccess) return e;
+    TppConst<NN, NMAT> kp;
+    for (int i = 0; i < NMAT + NN; ++i)
+        kp.v[i] = i < NMAT ? make_float4(0.f, 0.f, 0.f, 0.f) : m.kc_host[i - NMAT];
+    const unsigned grid = (unsigned)(w.grid > 0 ? w.grid : (int64_t)m.nscen * w.items);
+    kern<<<grid, Lay::B, Lay::bytes, s>>>(m, z, seed, path0, w, scr, kp);
+    return cudaGetLastError();
+}
+
+template <int NN, int NMAT, bool PHILOX>
+cudaError_t occ_tpq(int *blocks)
+{
+    using Lay = TpqLayout<NN, NMAT>;
+    auto kern = k_tpq<NN, NMAT, PHILOX>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::bytes);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kern, Lay::B, Lay::bytes);
+}
+
 template <int NN, int NMAT, bool PHILOX, Mode MODE>
 cudaError_t launch_tpp(const DevModel &m, const float *z, uint64_t seed, int64_t path0,
                        const Work &w, float *tape, const double *vbar, cudaStream_t s)
@@ -1120,6 +1486,29 @@ cudaError_t occ_tpp(int *blocks)
 bool f32_tpp_supports(int nn, int nmat) { return nn == 80 && nmat == 40; }
 
 int tps_block_threads() { return LMM_TPS_BLOCK; }
+
+bool f32_tpq_supports(int nn, int nmat) { return nn == 160 && nmat == 120; }
+
+int tpq_block_threads() { return LMM_TPQ_BLOCK; }
+
+size_t tpq_scratch_floats_per_block(int nn, int nmat, int ckpt)
+{
+    const int H = 40, Q = nn / H;
+    const int nck = ckpt > 0 ? (nmat - 1) / ckpt : 0;
+    return (size_t)(Q * nmat + (Q - 1) * nmat + 2 * (nn - H) + (size_t)nck * nn) * LMM_TPQ_BLOCK;
+}
+
+cudaError_t tpq_blocks_per_sm(bool philox, int *blocks)
+{
+    return philox ? occ_tpq<160, 120, true>(blocks) : occ_tpq<160, 120, false>(blocks);
+}
+
+cudaError_t launch_tpq_any(const DevModel &m, const float *z, uint64_t seed, int64_t path0, bool philox,
+                           const Work &w, float *scratch, cudaStream_t s)
+{
+    return philox ? launch_tpq<160, 120, true>(m, z, seed, path0, w, scratch, s)
+                  : launch_tpq<160, 120, false>(m, z, seed, path0, w, scratch, s);
+}
 
 size_t tps_scratch_floats_per_block(int nn, int nmat) { return (size_t)(2 * nmat + nn) * LMM_TPS_BLOCK; }
 

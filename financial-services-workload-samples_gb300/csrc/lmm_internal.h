@@ -70,6 +70,15 @@ size_t tps_scratch_floats_per_block(int nn, int nmat);
 cudaError_t tps_blocks_per_sm(bool philox, int *blocks);
 cudaError_t launch_tps_any(const DevModel &m, const float *z, uint64_t seed, int64_t path0, bool philox,
                            const Work &w, float *scratch, cudaStream_t s);
+// The fused 160/120 kernel with one thread per path and the reverse in passes
+// over blocks of 40 rates (lmm_f32_tpp.cu, k_tpq): a per-block scratch of
+// tpq_scratch_floats_per_block floats; checkpoint intervals multiples of 4.
+bool f32_tpq_supports(int nn, int nmat);
+int tpq_block_threads();
+size_t tpq_scratch_floats_per_block(int nn, int nmat, int ckpt);
+cudaError_t tpq_blocks_per_sm(bool philox, int *blocks);
+cudaError_t launch_tpq_any(const DevModel &m, const float *z, uint64_t seed, int64_t path0, bool philox,
+                           const Work &w, float *scratch, cudaStream_t s);
 // FP32 kernels with two threads per path (lmm_f32_tp2.cu): nn=160, nmat=120.
 // The forward/backward pair's tape: [nn][total] terminal inverse rates,
 // [nmat][total] full drift sums, [nmat][total] drift sums at rate nn/2 - 1.

@@ -60,7 +60,7 @@ def test_interval_changes_only_rounding(P):
     with P.Engine(cfg) as e:
         assert e.checkpoint_interval == 8
         g8, _ = e.greeks_f32(z)
-        e.set_checkpoint_interval(2)
+        e.set_checkpoint_interval(4)
         g2, _ = e.greeks_f32(z)
         e.set_checkpoint_interval(8)
         g8b, _ = e.greeks_f32(z)
@@ -71,8 +71,9 @@ def test_interval_changes_only_rounding(P):
 
 def test_interval_errors(P):
     """80/40 keeps every drift sum on chip and takes no rate checkpoints; the
-    160/120 thread pair runs steps in pairs (even k only); k must lie in
-    [0, nmat]. A refused setting leaves the interval as it was."""
+    160/120 kernels restore checkpoints between step pairs or groups of four
+    (odd k is refused either way); k must lie in [0, nmat]. A refused setting
+    leaves the interval as it was."""
     with P.Engine(cfgs().workload(2, 64)) as e:
         assert e.checkpoint_interval == 0
         e.set_checkpoint_interval(0)

@@ -315,3 +315,82 @@ def test_split_reverse_half_windows(ch):
     for step in range(TPP_NMAT):
         for rate in range(step + 1, TPP_NN):
             assert seen.get((step, rate)) == 1, (step, rate, seen.get((step, rate)))
+
+
+def block_window(n, G, ch, p, H, lo):
+    """Replays rev_block_window (csrc/lmm_f32_tpp.cu, k_tpq): steps n..n-G+1
+    over rates lo..lo+H-1 with the block's offset at run time. Returns the
+    flushes as (row k, set of cells) and the constant rows (as k) loaded."""
+    W = 2 * G - 1 + p
+    jmax = H + G - 2
+    full = lo > n
+    slots = {}
+    flushes, consts = [], set(range(H - p, jmax + 1))
+    for j in range(H, jmax + 1):
+        slots[j % W] = (j, set())
+    imin = n - 2 * G + 3 - lo
+    q = 0
+    while q * ch < H + G - 1:
+        top = H - 1 - q * ch
+        if not full and top < imin:
+            return flushes, {lo + j - n - 1 for j in consts}
+        i = top
+        while i > top - ch and i >= -(G - 1):
+            if i - p >= 0:
+                consts.add(i - p)
+            if i >= 0:
+                slots[i % W] = (i, set())
+            for g in range(G):
+                if 0 <= i + g <= H - 1:
+                    j = i + 2 * g
+                    sj, cells = slots[j % W]
+                    assert sj == j, (lo, n, i, g, sj, j)
+                    cells.add((n - g, lo + i + g))
+            jf = i + 2 * (G - 1)
+            if 0 <= jf <= jmax:
+                sj, cells = slots[jf % W]
+                assert sj == jf
+                flushes.append((lo + jf - n - 1, set(cells)))
+            i -= 1
+        q += 1
+    if full:
+        for j in range(G - 1):
+            sj, cells = slots[j % W]
+            assert sj == j
+            flushes.append((lo + j - n - 1, set(cells)))
+    return flushes, {lo + j - n - 1 for j in consts}
+
+
+@pytest.mark.parametrize("ch", [2, 4])
+def test_long_tenor_block_passes(ch):
+    """k_tpq at NN=160, NMAT=120: the blocks of 40 rates from the top, each
+    over its groups of four steps from the first group with an active cell,
+    flush every active cell exactly once to its own row; every row lies in
+    -VPAD..NN-1 and every constant row in -NMAT..NN-1; the groups a block skips
+    have no active cell in it, and the block below skips them too (so it never
+    reads a suffix sum the block above did not leave)."""
+    NN, NMAT, G, p, H, VP = 160, 120, 4, 1, 40, 4
+    seen = {}
+    first = {}
+    for b in range(NN // H - 1, -1, -1):
+        lo = b * H
+        n0 = NMAT - 1
+        while lo + H - 1 <= n0 - G + 1:
+            n0 -= G
+        first[b] = n0
+        for n in range(NMAT - 1, n0, -G):           # skipped groups: no active cell in the block
+            assert all(r <= m for m in range(n - G + 1, n + 1) for r in range(lo, lo + H))
+        for n in range(n0, 0, -G):
+            flushes, consts = block_window(n, G, ch, p, H, lo)
+            assert all(-NMAT <= k <= NN - 1 for k in consts), (lo, n)
+            for k, cells in flushes:
+                assert -VP <= k <= NN - 1, (lo, n, k)
+                for step, rate in cells:
+                    if rate > step:
+                        assert k == rate - step - 1, (lo, n, step, rate, k)
+                        seen[(step, rate)] = seen.get((step, rate), 0) + 1
+    for b in range(1, NN // H):
+        assert first[b - 1] <= first[b]
+    for step in range(NMAT):
+        for rate in range(step + 1, NN):
+            assert seen.get((step, rate)) == 1, (step, rate, seen.get((step, rate)))
