@@ -199,7 +199,7 @@ int f32_family(const lmm_engine *e)
 // 7 (one thread per path, the reverse in passes over blocks of 40 rates,
 // k_tpq) for fused 160/120 calls (LMM_USE_TPQ); the pair keeps family 5.
 #ifndef LMM_USE_TPQ
-#define LMM_USE_TPQ 0
+#define LMM_USE_TPQ 1
 #endif
 int family_for(const lmm_engine *e, Mode mode)
 {
