@@ -1104,9 +1104,12 @@ cudaError_t occ_tps(int *blocks)
 // the checkpoint at group boundaries. At most 40 rates and 40 log-adjoints
 // are live in the reverse, the other blocks wait in a per-block scratch, and
 // one copy of the 40-position reverse body serves every block (the block's
-// offset is a runtime value). Against two threads per path (k_tp2) there is
-// no pair to balance and no barrier per round: the same cells run with the
-// occupancy and schedule of the 80/40 kernels.
+// offset is a runtime value). The loads of the rates a group hands on (a
+// checkpoint, or the block below's parked rates) are issued inside the
+// group's body, each right after the group's last cell on its rate, so their
+// latency overlaps the rest of the body and the next group's top positions.
+// Against two threads per path (k_tp2) there is no pair to balance and no
+// barrier per round; the warps of a block run without barriers.
 // Scratch per block of the wave, rows of B floats (one per thread):
 // [Q][NMAT] block-top drift sums, [Q-1][NMAT] block-bottom suffix sums,
 // [NN-H] parked inverse rates of the lower blocks, [NN-H] deltas of the upper
@@ -1114,6 +1117,17 @@ cudaError_t occ_tps(int *blocks)
 // ---------------------------------------------------------------------------
 #ifndef LMM_TPQ_BLOCK
 #define LMM_TPQ_BLOCK 256
+#endif
+// Block barriers of the long-tenor fused kernel: one every LMM_TPQ_FSYNC
+// forward step pairs and every LMM_TPQ_RSYNC reverse step groups (0: none).
+// GB300, 160/120, 1,048,576 paths, rates saved every 8 steps: none 15.76 ms;
+// every second pair 16.17; every second or fourth group 16.01, 15.99; every
+// second pair and every group 17.20.
+#ifndef LMM_TPQ_FSYNC
+#define LMM_TPQ_FSYNC 0
+#endif
+#ifndef LMM_TPQ_RSYNC
+#define LMM_TPQ_RSYNC 0
 #endif
 
 template <int NN, int NMAT>
@@ -1184,10 +1198,13 @@ __device__ __forceinline__ void fwd_pair_window_caps(float (&IL)[NN], const floa
 // flushes the vega slots of positions 0 .. G-2 (they hold active cells);
 // otherwise it is left at the first chunk wholly below the lowest active
 // position, as rev_group_window, and the slots still open hold no-op cells
-// of spare rows.
+// of spare rows. Rates that the caller replaces after the group (positions
+// j > tl, from rs[j*B]) are loaded as soon as the group's last cell on them
+// is done, position j - G + 1, so that the loads overlap the rest of the
+// body; every such position lies at or above the lowest active one.
 template <int H, int B, int G, int CH, int P>
 __device__ __forceinline__ void rev_block_window(float (&X)[H], float (&Pb)[H], RevStep (&st)[G], float delta,
-                                                 int n, int LO)
+                                                 int n, int LO, const float *rs, int tl)
 {
     constexpr int JMAX = H + G - 2;
     constexpr int W = 2 * G - 1 + P;
@@ -1219,6 +1236,8 @@ __device__ __forceinline__ void rev_block_window(float (&X)[H], float (&Pb)[H], 
             }
             const int jf = i + 2 * (G - 1);
             if (jf >= 0 && jf <= JMAX) vg[jf * B] += A[jf % W];
+            const int jr = i + G - 1;
+            if (jr >= 0 && jr <= H - 1 && jr > tl) X[jr] = rs[jr * B];
         }
     }
     if (full) {
@@ -1237,6 +1256,7 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     constexpr int G = LMM_TPP_SKEW, RCH = PHILOX ? LMM_TPP_RCHUNK_PHILOX : LMM_TPP_RCHUNK;
     static_assert(NMAT % 4 == 0 && NMAT % G == 0 && H % G == 0, "normals in quads, reverse steps in groups");
     static_assert(RCH - 1 <= Lay::VPAD, "the windows' spare vega rows lie inside the table");
+    constexpr int kFsync = LMM_TPQ_FSYNC > 0 ? LMM_TPQ_FSYNC : 1, kRsync = LMM_TPQ_RSYNC > 0 ? LMM_TPQ_RSYNC : 1;
     extern __shared__ __align__(16) unsigned char smem[];
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
@@ -1291,8 +1311,7 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 for (int i = 0; i < NN; ++i) IL[i] = il0_s[i];
                 float4 zq, zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
                 for (int n = 0; n < NMAT; n += 2) {
-                    if (LMM_TPP_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0)
-                        __syncthreads();
+                    if (LMM_TPQ_FSYNC && (n % (2 * kFsync)) == 0) __syncthreads();
                     if ((n & 3) == 0) {
                         zq = zq_next;
                         if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
@@ -1337,12 +1356,9 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             // ---- reverse: the blocks from the top, each over its groups of steps ----
             for (int b = Q - 1; b >= 0; --b) {
                 const int LO = b * H;
-                if (b < Q - 1) {
+                if (b < Q - 1) {          // X holds the block's parked rates (the last group above loaded them)
 #pragma unroll
-                    for (int i = 0; i < H; ++i) {
-                        X[i] = sc[(Lay::s_il + LO + i) * B];
-                        Pb[i] = vs * rcp_approx(X[i] + delta);
-                    }
+                    for (int i = 0; i < H; ++i) Pb[i] = vs * rcp_approx(X[i] + delta);
                 }
                 // the block's first group with an active cell (its top rate above the group's lowest step)
                 int n0 = NMAT - 1;
@@ -1354,7 +1370,7 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                     ns[g] = b < Q - 1 ? sc[(Lay::s_sb + b * NMAT + n0 - g) * B] : 0.0f;
                 }
                 for (int n = n0; n > 0; n -= G) {
-                    if (LMM_TPP_SYNC) __syncthreads();
+                    if (LMM_TPQ_RSYNC && ((n0 - n) / G) % kRsync == 0) __syncthreads();
                     RevStep st[G];
 #pragma unroll
                     for (int g = 0; g < G; ++g) {
@@ -1372,18 +1388,23 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                             ns[g] = b < Q - 1 ? sc[(Lay::s_sb + b * NMAT + n - G - g) * B] : 0.0f;
                         }
                     }
-                    rev_block_window<H, B, G, RCH, kPref<PHILOX>>(X, Pb, st, delta, n, LO);
+                    // the rates the group hands on that come from memory: a checkpoint at
+                    // its end time t (the reverse of steps >= t leaves rates i <= t
+                    // untouched), or in a block's last group the block below's parked rates
+                    const int t = n - G + 1;
+                    const float *rs = sc;
+                    int tl = H;
+                    if (nck > 0 && t % ckd == 0 && t >= ck) {
+                        rs = ckp + (size_t)((t / ckd - 1) * NN + LO) * B;
+                        tl = t - LO;
+                    } else if (b > 0 && n - G <= 0) {
+                        rs = sc + (size_t)(Lay::s_il + LO - H) * B;
+                        tl = -1;
+                    }
+                    rev_block_window<H, B, G, RCH, kPref<PHILOX>>(X, Pb, st, delta, n, LO, rs, tl);
                     if (b > 0) {
 #pragma unroll
                         for (int g = 0; g < G; ++g) sc[(Lay::s_sb + (b - 1) * NMAT + n - g) * B] = st[g].S;
-                    }
-                    const int t = n - G + 1;          // the time the group leaves the rates at
-                    if (nck > 0 && t % ckd == 0 && t >= ck) {
-                        // the reverse of steps >= t leaves rates i <= t untouched
-                        const int c = t / ckd - 1;
-#pragma unroll
-                        for (int i = 0; i < H; ++i)
-                            if (LO + i > t) X[i] = ckp[(c * NN + LO + i) * B];
                     }
                 }
                 if (b > 0) {

@@ -317,10 +317,13 @@ def test_split_reverse_half_windows(ch):
             assert seen.get((step, rate)) == 1, (step, rate, seen.get((step, rate)))
 
 
-def block_window(n, G, ch, p, H, lo):
+def block_window(n, G, ch, p, H, lo, tl=None):
     """Replays rev_block_window (csrc/lmm_f32_tpp.cu, k_tpq): steps n..n-G+1
     over rates lo..lo+H-1 with the block's offset at run time. Returns the
-    flushes as (row k, set of cells) and the constant rows (as k) loaded."""
+    flushes as (row k, set of cells) and the constant rows (as k) loaded.
+    With tl given, also checks the in-body loads of the rates the caller
+    replaces (local positions j > tl): each comes after the group's last
+    cell on its rate, and every such position is loaded once."""
     W = 2 * G - 1 + p
     jmax = H + G - 2
     full = lo > n
@@ -329,11 +332,18 @@ def block_window(n, G, ch, p, H, lo):
     for j in range(H, jmax + 1):
         slots[j % W] = (j, set())
     imin = n - 2 * G + 3 - lo
+    loaded = set()
+
+    def done():
+        if tl is not None:
+            assert loaded == set(range(max(tl + 1, 0), H)), (lo, n, tl, sorted(loaded))
+        return flushes, {lo + j - n - 1 for j in consts}
+
     q = 0
     while q * ch < H + G - 1:
         top = H - 1 - q * ch
         if not full and top < imin:
-            return flushes, {lo + j - n - 1 for j in consts}
+            return done()
         i = top
         while i > top - ch and i >= -(G - 1):
             if i - p >= 0:
@@ -346,11 +356,16 @@ def block_window(n, G, ch, p, H, lo):
                     sj, cells = slots[j % W]
                     assert sj == j, (lo, n, i, g, sj, j)
                     cells.add((n - g, lo + i + g))
+                    assert i + g not in loaded, (lo, n, i, g)   # no cell after the rate's load
             jf = i + 2 * (G - 1)
             if 0 <= jf <= jmax:
                 sj, cells = slots[jf % W]
                 assert sj == jf
                 flushes.append((lo + jf - n - 1, set(cells)))
+            jr = i + G - 1
+            if tl is not None and 0 <= jr <= H - 1 and jr > tl:
+                assert jr not in loaded
+                loaded.add(jr)
             i -= 1
         q += 1
     if full:
@@ -358,7 +373,7 @@ def block_window(n, G, ch, p, H, lo):
             sj, cells = slots[j % W]
             assert sj == j
             flushes.append((lo + j - n - 1, set(cells)))
-    return flushes, {lo + j - n - 1 for j in consts}
+    return done()
 
 
 @pytest.mark.parametrize("ch", [2, 4])
@@ -394,3 +409,46 @@ def test_long_tenor_block_passes(ch):
     for step in range(NMAT):
         for rate in range(step + 1, NN):
             assert seen.get((step, rate)) == 1, (step, rate, seen.get((step, rate)))
+
+
+@pytest.mark.parametrize("ck", [0, 4, 8, 12, 16, 40, 116])
+@pytest.mark.parametrize("ch", [2, 4])
+def test_long_tenor_checkpoints_and_hand_on_loads(ck, ch):
+    """k_tpq's rate checkpoints every ck steps (ck a multiple of 4; 0: none)
+    and the rates each group loads for the next: the forward saves
+    checkpoint c after step (c+1)ck - 1 for the rates above (c+1)ck; a group
+    ending at a checkpoint time t loads, inside its body and after its last
+    cell on each, the block's rates above t from that checkpoint, only rates
+    the forward saved and rows inside the scratch; a block's last group
+    loads all of the parked rates of the block below, and no group has both
+    loads."""
+    NN, NMAT, G, H, p = 160, 120, 4, 40, 1
+    nck = (NMAT - 1) // ck if ck else 0
+    ckd = ck if ck else 1
+    saved = set()
+    for n in range(0, NMAT, 2):
+        if nck > 0 and (n + 2) % ckd == 0 and n + 2 < NMAT:
+            c = (n + 2) // ckd - 1
+            assert 0 <= c < nck
+            saved |= {(c, i) for i in range(NN) if i > n + 2}
+    for b in range(NN // H - 1, -1, -1):
+        lo = b * H
+        n0 = NMAT - 1
+        while lo + H - 1 <= n0 - G + 1:
+            n0 -= G
+        parked = 0
+        for n in range(n0, 0, -G):
+            t = n - G + 1
+            tl = H
+            if nck > 0 and t % ckd == 0 and t >= ck:
+                c = t // ckd - 1
+                assert 0 <= c < nck and 0 <= c * NN + lo and c * NN + lo + H <= nck * NN
+                tl = t - lo
+                assert all((c, lo + j) in saved for j in range(max(tl + 1, 0), H)), (b, n, c)
+                assert not (b > 0 and n - G <= 0)
+            elif b > 0 and n - G <= 0:
+                tl = -1
+                parked += 1
+                assert lo > n                    # a full window: every position is loaded
+            block_window(n, G, ch, p, H, lo, tl)
+        assert parked == (1 if b > 0 else 0), b
