@@ -478,8 +478,8 @@ def run_ours(args):
                 others[c.name] = {"paths_per_s": c.nscen * c.paths / (kms * 1e-3), "ms": kms,
                                   "nn": c.nn, "nmat": c.nmat, "scenarios": c.nscen, "normals": mode,
                                   "kernel": "k_tps (thread per path, reverse split over the rate halves)" if c.nn == 80 else
-                                  "k_tp2 (two threads per path in alternating blocks of 40 rates; reverse "
-                                  "rebuilt from each block's top drift sums, rates saved every 8 steps)"}
+                                  "k_tpq (thread per path; reverse in passes over blocks of 40 rates, rebuilt "
+                                  "from each block's top drift sums, rates saved every 8 steps)"}
                 del zw
 
     # ---- roofline -----------------------------------------------------------

@@ -291,11 +291,27 @@ __device__ __forceinline__ void kahan_add_bf16c(float &s, unsigned short &cb, fl
     s = t;
 }
 
+// 1: the reverse windows keep d = -delta*lambda_k beside each constant of
+// their ring (one multiply per position, shared by the G cells of the
+// position), and the cell forms lambda(1 - delta t) as one FMA,
+// fma(d, t, lambda), instead of an FMA and a multiply. Per kernel: k_tpp,
+// k_tps, k_tpq.
+#ifndef LMM_TPP_DCONST
+#define LMM_TPP_DCONST 1
+#endif
+#ifndef LMM_TPS_DCONST
+#define LMM_TPS_DCONST 1
+#endif
+#ifndef LMM_TPQ_DCONST
+#define LMM_TPQ_DCONST 0
+#endif
+
 // One reverse cell (path_calc_b2 :105-111 in log-adjoint form) + vega, with
-// its constants and vega partial sum passed in from the window.
-template <int NN>
+// its constants (k, and d = -delta*k.w with DC) and vega partial sum
+// passed in from the window.
+template <int NN, bool DC>
 __device__ __forceinline__ void rev_cell(float (&IL)[NN], float (&Pb)[NN], RevStep &s, int i,
-                                         const float4 &k, float &acc, float delta)
+                                         const float4 &k, float d, float &acc, float delta)
 {
     const float y = kYrun ? s.V : s.V + s.sqez;
     const float iln = IL[i] * ex2_approx(fmaf(k.x, y, k.y));
@@ -304,8 +320,13 @@ __device__ __forceinline__ void rev_cell(float (&IL)[NN], float (&Pb)[NN], RevSt
     const float pb = Pb[i];
     s.S = fmaf(k.z, pb, s.S);
     const float tS = t * s.S;
-    acc += fmaf(pb, fmaf(-delta, k.w, y), tS);
-    Pb[i] = fmaf(k.w * fmaf(-delta, t, 1.0f), tS, pb);
+    if (DC) {
+        acc += fmaf(pb, y + d, tS);
+        Pb[i] = fmaf(fmaf(d, t, k.w), tS, pb);
+    } else {
+        acc += fmaf(pb, fmaf(-delta, k.w, y), tS);
+        Pb[i] = fmaf(k.w * fmaf(-delta, t, 1.0f), tS, pb);
+    }
     IL[i] = iln;
 }
 
@@ -334,10 +355,12 @@ __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN
     float *vg = st[0].vg;
     unsigned short *vc = st[0].vc;
     float4 C[W];
+    float D[W];
     float A[W];
 #pragma unroll
     for (int j = NN - P; j <= JMAX; ++j) {
         C[j % W] = kc[j];
+        D[j % W] = -delta * C[j % W].w;
         if (j >= NN) A[j % W] = 0.0f;
     }
     const int imin = n - 2 * G + 3;
@@ -347,13 +370,16 @@ __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN
         if (top < imin) return;
 #pragma unroll
         for (int i = top; i > top - CH && i >= -(G - 1); --i) {
-            if (i - P >= 1) C[(i - P) % W] = kc[i - P];
+            if (i - P >= 1) {
+                C[(i - P) % W] = kc[i - P];
+                D[(i - P) % W] = -delta * C[(i - P) % W].w;
+            }
             if (i >= 1) A[i % W] = 0.0f;
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 if (i + g >= 1 && i + g <= NN - 1) {
                     const int j = i + 2 * g;
-                    rev_cell<NN>(IL, Pb, st[g], i + g, C[j % W], A[j % W], delta);
+                    rev_cell<NN, LMM_TPP_DCONST != 0>(IL, Pb, st[g], i + g, C[j % W], D[j % W], A[j % W], delta);
                 }
             }
             const int jf = i + 2 * (G - 1);
@@ -377,20 +403,13 @@ __device__ __forceinline__ void rev_group_window(float (&IL)[NN], float (&Pb)[NN
 // GB300). Returns the discounted value; *disc_out receives the discount
 // factor, *mask_out which swaptions (in grouped order) paid, and Bst[m*B] (if
 // given) the annuity factors B[m] of :139 rounded to FP32, for the adjoint.
-template <int NN, int NMAT, int B>
-__device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float delta, const int *ost,
-                                                const F2 *oKd, const float *oWf, float *disc_out,
-                                                float *Bst, float *ILst, unsigned long long *mask_out)
+// payoff_forward_staged is its annuity part, from the discount product
+// `disc` and the M annuity rates staged in ILst[m*B].
+template <int M, int B>
+__device__ __forceinline__ float payoff_forward_staged(F2 disc, float delta, const int *ost, const F2 *oKd,
+                                                       const float *oWf, float *disc_out, float *Bst,
+                                                       const float *ILst, unsigned long long *mask_out)
 {
-    constexpr int M = NN - NMAT;
-    F2 disc{1.0f, 0.0f};
-#pragma unroll
-    for (int n = 0; n < NMAT; ++n) disc = f2_mul(disc, bond_ratio(IL[n], delta));
-    // The annuity recursion runs as a rolled loop over the rates staged in
-    // shared memory: one copy of its code instead of one per maturity
-    // (instruction cache).
-#pragma unroll
-    for (int m = 0; m < M; ++m) ILst[m * B] = IL[NMAT + m];
     F2 b{1.0f, 0.0f}, sb{0.0f, 0.0f}, vs{0.0f, 0.0f};
     unsigned long long mask = 0ull;
 #pragma unroll 1
@@ -412,6 +431,23 @@ __device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float del
     *mask_out = mask;
     const F2 v = f2_mul(vs, disc);
     return __fadd_rn(v.hi, v.lo);
+}
+
+template <int NN, int NMAT, int B>
+__device__ __forceinline__ float payoff_forward(const float (&IL)[NN], float delta, const int *ost,
+                                                const F2 *oKd, const float *oWf, float *disc_out,
+                                                float *Bst, float *ILst, unsigned long long *mask_out)
+{
+    constexpr int M = NN - NMAT;
+    F2 disc{1.0f, 0.0f};
+#pragma unroll
+    for (int n = 0; n < NMAT; ++n) disc = f2_mul(disc, bond_ratio(IL[n], delta));
+    // The annuity recursion runs as a rolled loop over the rates staged in
+    // shared memory: one copy of its code instead of one per maturity
+    // (instruction cache).
+#pragma unroll
+    for (int m = 0; m < M; ++m) ILst[m * B] = IL[NMAT + m];
+    return payoff_forward_staged<M, B>(disc, delta, ost, oKd, oWf, disc_out, Bst, ILst, mask_out);
 }
 
 // Payoff adjoint, portfolio_b :173-184 (with the rate and its adjoint kept
@@ -842,10 +878,12 @@ __device__ __forceinline__ void rev_half_window(float (&X)[H], float (&Pb)[H], R
     const float4 *kc = st[0].kc;
     float *vg = st[0].vg;
     float4 C[W];
+    float D[W];
     float A[W];
 #pragma unroll
     for (int j = H - P; j <= JMAX; ++j) {
         C[j % W] = kc[j];
+        D[j % W] = -delta * C[j % W].w;
         if (j >= H) A[j % W] = 0.0f;
     }
     const int imin = n - 2 * G + 3 - LO;     // lowest local position with an active cell
@@ -855,13 +893,16 @@ __device__ __forceinline__ void rev_half_window(float (&X)[H], float (&Pb)[H], R
         if (LO == 0 && top < imin) return;
 #pragma unroll
         for (int i = top; i > top - CH && i >= -(G - 1); --i) {
-            if (i - P >= (LO > 0 ? 0 : 1)) C[(i - P) % W] = kc[i - P];
+            if (i - P >= (LO > 0 ? 0 : 1)) {
+                C[(i - P) % W] = kc[i - P];
+                D[(i - P) % W] = -delta * C[(i - P) % W].w;
+            }
             if (i >= (LO > 0 ? 0 : 1)) A[i % W] = 0.0f;
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 if (i + g >= (LO > 0 ? 0 : 1) && i + g <= H - 1) {
                     const int j = i + 2 * g;
-                    rev_cell<H>(X, Pb, st[g], i + g, C[j % W], A[j % W], delta);
+                    rev_cell<H, LMM_TPS_DCONST != 0>(X, Pb, st[g], i + g, C[j % W], D[j % W], A[j % W], delta);
                 }
             }
             const int jf = i + 2 * (G - 1);
@@ -1115,6 +1156,13 @@ cudaError_t occ_tps(int *blocks)
 // [NN-H] parked inverse rates of the lower blocks, [NN-H] deltas of the upper
 // blocks, [NCK][NN] rate checkpoints.
 // ---------------------------------------------------------------------------
+// 1: the forward in two passes over 80 rates each (the lower rates for every
+// step, then the upper ones from the drift sums the first pass left at rate
+// 79), so that at most 80 rates are live in registers; 0: all 160 rates in
+// registers. GB300, 1,048,576 paths: 15.69 -> 15.49 ms.
+#ifndef LMM_TPQ_FPASS
+#define LMM_TPQ_FPASS 1
+#endif
 #ifndef LMM_TPQ_BLOCK
 #define LMM_TPQ_BLOCK 256
 #endif
@@ -1125,6 +1173,26 @@ cudaError_t occ_tps(int *blocks)
 // second pair and every group 17.20.
 #ifndef LMM_TPQ_FSYNC
 #define LMM_TPQ_FSYNC 0
+#endif
+// Steps per reverse group, reverse and forward chunk lengths and the constant
+// prefetch distance of the long-tenor fused kernel (as LMM_TPP_*).
+#ifndef LMM_TPQ_SKEW
+#define LMM_TPQ_SKEW LMM_TPP_SKEW
+#endif
+#ifndef LMM_TPQ_RCHUNK
+#define LMM_TPQ_RCHUNK LMM_TPP_RCHUNK
+#endif
+#ifndef LMM_TPQ_RCHUNK_PHILOX
+#define LMM_TPQ_RCHUNK_PHILOX LMM_TPP_RCHUNK_PHILOX
+#endif
+#ifndef LMM_TPQ_CHUNK
+#define LMM_TPQ_CHUNK LMM_TPP_CHUNK
+#endif
+#ifndef LMM_TPQ_PREF
+#define LMM_TPQ_PREF LMM_TPP_PREF
+#endif
+#ifndef LMM_TPQ_PREF_PHILOX
+#define LMM_TPQ_PREF_PHILOX LMM_TPP_PREF_PHILOX
 #endif
 #ifndef LMM_TPQ_RSYNC
 #define LMM_TPQ_RSYNC 0
@@ -1147,6 +1215,7 @@ struct TpqLayout {
     static constexpr int vg = align16(okk + 8 * kMaxNopt);           // float[VPAD+NN][B] vega rows
     static constexpr int acc = align16(vg + 4 * (VPAD + NN) * B);    // double[NW][2*NOUT]
     static constexpr int bytes = acc + 8 * NW * 2 * NOUT;
+    static_assert(bytes <= 227 * 1024, "one block's shared memory");
     static constexpr int s_vt = 0, s_sb = Q * NMAT, s_il = s_sb + (Q - 1) * NMAT, s_d = s_il + NN - H,
                          s_ck = s_d + NN - H;
     static_assert(NN % H == 0 && M == H && H % 4 == 0, "the top block is the annuity rates");
@@ -1190,6 +1259,48 @@ __device__ __forceinline__ void fwd_pair_window_caps(float (&IL)[NN], const floa
     fwd_cell(IL[NN - 1], V1, C[(NN - 2) % R], sqez1, delta);
 }
 
+// Forward steps n and n+1 over the NP rates LO .. LO+NP-1 held in IL[] at
+// local positions 0 .. NP-1, paired as fwd_pair_window: cell (n, p) with
+// cell (n+1, p-1). V0, V1 enter as the steps' drift sums below the pass (at
+// rate LO-1; the normal term alone for LO = 0) and leave as the sums at its
+// top rate; V0c[q], V1c[q] return the sums at local position qH + H-1, the
+// top rate of each H-rate block of the pass. kcn points at step n's
+// constants for local position 0 (k = LO - n - 1; the NMAT zero rows below
+// k = 0 make the inactive cells exact no-ops); nrel = n - LO < NP - 1.
+template <int NP, int H, int CH, int P>
+__device__ __forceinline__ void fwd_pair_pass(float (&IL)[NP], const float4 *kcn, float delta, int nrel,
+                                              float &V0, float &V1, float (&V0c)[NP / H], float (&V1c)[NP / H])
+{
+    constexpr int R = 3 + P;
+    float4 C[R];
+#pragma unroll
+    for (int q = 0; q < NP / H; ++q) {
+        V0c[q] = V0;
+        V1c[q] = V1;
+    }
+    const int c0 = nrel + 1 > 0 ? (nrel + 1) / CH : 0;
+#pragma unroll
+    for (int c = 0; c * CH < NP; ++c) {
+        if (c >= c0) {
+            if (c == c0) {
+#pragma unroll
+                for (int j = c * CH - 2; j < c * CH + P; ++j)
+                    if (j < NP) C[(j % R + R) % R] = kcn[j];
+            }
+#pragma unroll
+            for (int p = c * CH; p < (c + 1) * CH && p < NP; ++p) {
+                if (p + P < NP) C[(p + P) % R] = kcn[p + P];
+                fwd_cell(IL[p], V0, C[p % R], 0.0f, delta);
+                if (p >= 1) fwd_cell(IL[p - 1], V1, C[((p - 2) % R + R) % R], 0.0f, delta);
+                if (p % H == H - 1) V0c[p / H] = V0;
+                if (p >= 1 && (p - 1) % H == H - 1) V1c[(p - 1) / H] = V1;
+            }
+        }
+    }
+    fwd_cell(IL[NP - 1], V1, C[(NP - 2) % R], 0.0f, delta);
+    V1c[NP / H - 1] = V1;
+}
+
 // Reverse steps n .. n-G+1 over the block of H rates LO .. LO+H-1 (X[], Pb[]
 // at local positions 0 .. H-1; LO a runtime multiple of G): rev_group_window
 // on a block. st[0].kc and st[0].vg point at step n's constants and vega rows
@@ -1211,10 +1322,12 @@ __device__ __forceinline__ void rev_block_window(float (&X)[H], float (&Pb)[H], 
     const float4 *kc = st[0].kc;
     float *vg = st[0].vg;
     float4 C[W];
+    float D[W];
     float A[W];
 #pragma unroll
     for (int j = H - P; j <= JMAX; ++j) {
         C[j % W] = kc[j];
+        D[j % W] = -delta * C[j % W].w;
         if (j >= H) A[j % W] = 0.0f;
     }
     const bool full = LO > n;
@@ -1225,13 +1338,16 @@ __device__ __forceinline__ void rev_block_window(float (&X)[H], float (&Pb)[H], 
         if (!full && top < imin) return;
 #pragma unroll
         for (int i = top; i > top - CH && i >= -(G - 1); --i) {
-            if (i - P >= 0) C[(i - P) % W] = kc[i - P];
+            if (i - P >= 0) {
+                C[(i - P) % W] = kc[i - P];
+                D[(i - P) % W] = -delta * C[(i - P) % W].w;
+            }
             if (i >= 0) A[i % W] = 0.0f;
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 if (i + g >= 0 && i + g <= H - 1) {
                     const int j = i + 2 * g;
-                    rev_cell<H>(X, Pb, st[g], i + g, C[j % W], A[j % W], delta);
+                    rev_cell<H, LMM_TPQ_DCONST != 0>(X, Pb, st[g], i + g, C[j % W], D[j % W], A[j % W], delta);
                 }
             }
             const int jf = i + 2 * (G - 1);
@@ -1253,10 +1369,14 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 {
     using Lay = TpqLayout<NN, NMAT>;
     constexpr int B = Lay::B, H = Lay::H, Q = Lay::Q, M = Lay::M, NOUT = Lay::NOUT, PAD = NMAT;
-    constexpr int G = LMM_TPP_SKEW, RCH = PHILOX ? LMM_TPP_RCHUNK_PHILOX : LMM_TPP_RCHUNK;
+    constexpr int G = LMM_TPQ_SKEW, RCH = PHILOX ? LMM_TPQ_RCHUNK_PHILOX : LMM_TPQ_RCHUNK;
+    constexpr int PF = PHILOX ? LMM_TPQ_PREF_PHILOX : LMM_TPQ_PREF;
     static_assert(NMAT % 4 == 0 && NMAT % G == 0 && H % G == 0, "normals in quads, reverse steps in groups");
     static_assert(RCH - 1 <= Lay::VPAD, "the windows' spare vega rows lie inside the table");
     constexpr int kFsync = LMM_TPQ_FSYNC > 0 ? LMM_TPQ_FSYNC : 1, kRsync = LMM_TPQ_RSYNC > 0 ? LMM_TPQ_RSYNC : 1;
+    constexpr int HF = 2 * H;      // rates per forward pass (LMM_TPQ_FPASS)
+    static_assert(kYrun, "the drift sums carry the normal term");
+    static_assert(!LMM_TPQ_FPASS || (NN == 2 * HF && NMAT > HF && NMAT - HF + M == HF), "two forward passes");
     extern __shared__ __align__(16) unsigned char smem[];
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
@@ -1264,7 +1384,6 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     float *owf_s = reinterpret_cast<float *>(smem + Lay::owf);
     F2 *okk_s = reinterpret_cast<F2 *>(smem + Lay::okk);
     float *vg_s = reinterpret_cast<float *>(smem + Lay::vg);
-    double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int i = tid; i <= M; i += B) ost_s[i] = m.opt_start[i];
@@ -1273,7 +1392,6 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
         owf_s[i] = m.optWf[i];
         okk_s[i] = f2_from(m.optKd[i] * m.deltad);
     }
-    double *acc = acc_s + warp * 2 * NOUT;
     const float delta = m.delta, sqd = m.sqd;
     const float4 *kc0 = kp.v + PAD;
     float *vg0 = vg_s + Lay::VPAD * B + tid;
@@ -1282,6 +1400,8 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     const int ckd = ck > 0 ? ck : 1;
     const int64_t rows = Lay::s_ck + (int64_t)nck * NN;
     float *sc = scr + (size_t)blockIdx.x * rows * B + tid;          // sc[row * B]
+    double *acc_s = reinterpret_cast<double *>(smem + Lay::acc);     // [NW][2*NOUT]
+    double *acc = acc_s + warp * 2 * NOUT;
     float *ckp = sc + (size_t)Lay::s_ck * B;                         // checkpoint c, rate i: ckp[(c*NN + i)*B]
 
     const int units = m.nscen * w.items;
@@ -1304,6 +1424,100 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             float disc = 1.0f, V, vs;
             float X[H], Pb[H];        // the block in the reverse: inverse rates, log-adjoints
             unsigned long long mask = 0ull;
+#if LMM_TPQ_FPASS
+            {
+                // ---- forward (path_calc_b1 :34-82), pass 1: rates 0 .. HF-1 for every step ----
+                F2 dprod{1.0f, 0.0f};          // the discount product, rates 0 .. NMAT-1 in order
+                {
+                    float IL[HF];
+#pragma unroll
+                    for (int i = 0; i < HF; ++i) IL[i] = il0_s[i];
+                    float4 zq, zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
+                    for (int n = 0; n < NMAT; n += 2) {
+                        if (LMM_TPQ_FSYNC && (n % (2 * kFsync)) == 0) __syncthreads();
+                        if ((n & 3) == 0) {
+                            zq = zq_next;
+                            if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+                        }
+                        float V0 = sqd * ((n & 2) ? zq.z : zq.x);     // drift sums from the normal term (kYrun)
+                        float V1 = sqd * ((n & 2) ? zq.w : zq.y);
+                        float V0c[HF / H], V1c[HF / H];
+                        if (n < HF - 1) {
+                            fwd_pair_pass<HF, H, LMM_TPQ_CHUNK, PF>(IL, kc0 - (n + 1), delta, n, V0, V1, V0c, V1c);
+                        } else {                 // no rate of the pass moves
+#pragma unroll
+                            for (int q = 0; q < HF / H; ++q) {
+                                V0c[q] = V0;
+                                V1c[q] = V1;
+                            }
+                        }
+#pragma unroll
+                        for (int q = 0; q < HF / H; ++q) {
+                            sc[(Lay::s_vt + q * NMAT + n) * B] = V0c[q];
+                            sc[(Lay::s_vt + q * NMAT + n + 1) * B] = V1c[q];
+                        }
+                        if (nck > 0 && (n + 2) % ckd == 0 && n + 2 < HF - 1) {
+                            // rates i <= n+2 are final from here on: only the others are saved
+                            const int c = (n + 2) / ckd - 1;
+#pragma unroll
+                            for (int i = 0; i < HF; ++i)
+                                if (i > n + 2) ckp[(c * NN + i) * B] = IL[i];
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < HF; ++i) {
+                        dprod = f2_mul(dprod, bond_ratio(IL[i], delta));
+                        sc[(Lay::s_il + i) * B] = IL[i];
+                    }
+                }
+                // ---- pass 2: rates HF .. NN-1, each step from pass 1's drift sum at rate HF-1 ----
+                float IL[NN - HF];
+#pragma unroll
+                for (int i = 0; i < NN - HF; ++i) IL[i] = il0_s[HF + i];
+                const float *vin = sc + (size_t)(Lay::s_vt + (HF / H - 1) * NMAT) * B;
+                float nv0 = vin[0], nv1 = vin[B];
+                for (int n = 0; n < NMAT; n += 2) {
+                    if (LMM_TPQ_FSYNC && (n % (2 * kFsync)) == 0) __syncthreads();
+                    float V0 = nv0, V1 = nv1;
+                    if (n + 2 < NMAT) {
+                        nv0 = vin[(n + 2) * B];
+                        nv1 = vin[(n + 3) * B];
+                    }
+                    float V0c[(NN - HF) / H], V1c[(NN - HF) / H];
+                    fwd_pair_pass<NN - HF, H, LMM_TPQ_CHUNK, PF>(IL, kc0 - (n + 1) + HF, delta, n - HF, V0, V1, V0c,
+                                                                 V1c);
+#pragma unroll
+                    for (int q = 0; q < (NN - HF) / H; ++q) {
+                        sc[(Lay::s_vt + (HF / H + q) * NMAT + n) * B] = V0c[q];
+                        sc[(Lay::s_vt + (HF / H + q) * NMAT + n + 1) * B] = V1c[q];
+                    }
+                    if (nck > 0 && (n + 2) % ckd == 0 && n + 2 < NMAT) {
+                        const int c = (n + 2) / ckd - 1;
+#pragma unroll
+                        for (int i = 0; i < NN - HF; ++i)
+                            if (HF + i > n + 2) ckp[(c * NN + HF + i) * B] = IL[i];
+                    }
+                }
+                // ---- payoff (portfolio_b :133-171, :186-197) and the annuity adjoint ----
+#pragma unroll
+                for (int i = 0; i < NMAT - HF; ++i) {
+                    dprod = f2_mul(dprod, bond_ratio(IL[i], delta));
+                    sc[(Lay::s_il + HF + i) * B] = IL[i];
+                }
+                float *Bst = vg0;
+                float *ILst = vg0 + M * B;
+#pragma unroll
+                for (int m2 = 0; m2 < M; ++m2) ILst[m2 * B] = IL[NMAT - HF + m2];
+                V = payoff_forward_staged<M, B>(dprod, delta, ost_s, okk_s, owf_s, &disc, Bst, ILst, &mask);
+                payoff_adjoint_stage<NN, NMAT, B>(1.0f, disc, Bst, ILst, mask, delta, ost_s, okf_s, owf_s);
+#pragma unroll
+                for (int i = 0; i < H; ++i) {
+                    X[i] = IL[NN - HF - H + i];
+                    Pb[i] = ILst[i * B];
+                }
+                vs = -V * delta;
+            }
+#else
             {
                 // ---- forward over all NN rates (path_calc_b1 :34-82) ----
                 float IL[NN];
@@ -1319,7 +1533,7 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                     const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
                     const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
                     float V0, V1, V0c[Q - 1], V1c[Q - 1];
-                    fwd_pair_window_caps<NN, H, LMM_TPP_CHUNK, kPref<PHILOX>>(IL, kc0 - (n + 1), sqez0, sqez1, delta,
+                    fwd_pair_window_caps<NN, H, LMM_TPQ_CHUNK, PF>(IL, kc0 - (n + 1), sqez0, sqez1, delta,
                                                                              n, V0, V1, V0c, V1c);
 #pragma unroll
                     for (int b = 0; b < Q - 1; ++b) {
@@ -1350,6 +1564,7 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 for (int i = 0; i < NN - H; ++i) sc[(Lay::s_il + i) * B] = IL[i];
                 vs = -V * delta;
             }
+#endif
 #pragma unroll
             for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
 
@@ -1401,7 +1616,7 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                         rs = sc + (size_t)(Lay::s_il + LO - H) * B;
                         tl = -1;
                     }
-                    rev_block_window<H, B, G, RCH, kPref<PHILOX>>(X, Pb, st, delta, n, LO, rs, tl);
+                    rev_block_window<H, B, G, RCH, PF>(X, Pb, st, delta, n, LO, rs, tl);
                     if (b > 0) {
 #pragma unroll
                         for (int g = 0; g < G; ++g) sc[(Lay::s_sb + (b - 1) * NMAT + n - g) * B] = st[g].S;

@@ -376,15 +376,16 @@ def block_window(n, G, ch, p, H, lo, tl=None):
     return done()
 
 
+@pytest.mark.parametrize("G", [4, 8])
 @pytest.mark.parametrize("ch", [2, 4])
-def test_long_tenor_block_passes(ch):
+def test_long_tenor_block_passes(ch, G):
     """k_tpq at NN=160, NMAT=120: the blocks of 40 rates from the top, each
-    over its groups of four steps from the first group with an active cell,
+    over its groups of G steps from the first group with an active cell,
     flush every active cell exactly once to its own row; every row lies in
     -VPAD..NN-1 and every constant row in -NMAT..NN-1; the groups a block skips
     have no active cell in it, and the block below skips them too (so it never
     reads a suffix sum the block above did not leave)."""
-    NN, NMAT, G, p, H, VP = 160, 120, 4, 1, 40, 4
+    NN, NMAT, p, H, VP = 160, 120, 1, 40, 4
     seen = {}
     first = {}
     for b in range(NN // H - 1, -1, -1):
@@ -412,8 +413,8 @@ def test_long_tenor_block_passes(ch):
 
 
 @pytest.mark.parametrize("ck", [0, 4, 8, 12, 16, 40, 116])
-@pytest.mark.parametrize("ch", [2, 4])
-def test_long_tenor_checkpoints_and_hand_on_loads(ck, ch):
+@pytest.mark.parametrize("ch,G", [(2, 4), (4, 4), (2, 8), (4, 8)])
+def test_long_tenor_checkpoints_and_hand_on_loads(ck, ch, G):
     """k_tpq's rate checkpoints every ck steps (ck a multiple of 4; 0: none)
     and the rates each group loads for the next: the forward saves
     checkpoint c after step (c+1)ck - 1 for the rates above (c+1)ck; a group
@@ -422,7 +423,7 @@ def test_long_tenor_checkpoints_and_hand_on_loads(ck, ch):
     the forward saved and rows inside the scratch; a block's last group
     loads all of the parked rates of the block below, and no group has both
     loads."""
-    NN, NMAT, G, H, p = 160, 120, 4, 40, 1
+    NN, NMAT, H, p = 160, 120, 40, 1
     nck = (NMAT - 1) // ck if ck else 0
     ckd = ck if ck else 1
     saved = set()
@@ -452,3 +453,86 @@ def test_long_tenor_checkpoints_and_hand_on_loads(ck, ch):
                 assert lo > n                    # a full window: every position is loaded
             block_window(n, G, ch, p, H, lo, tl)
         assert parked == (1 if b > 0 else 0), b
+
+
+def fwd_pair_pass(NP, H, CH, P, LO, n, NMAT, NN, done):
+    """Replays fwd_pair_pass (csrc/lmm_f32_tpp.cu, k_tpq's forward passes):
+    steps n, n+1 over rates LO .. LO+NP-1. `done` maps a step to the rates
+    whose cells it has run (active or not), in order; the constant of every
+    cell must be its own k = rate - step - 1 and lie in the table
+    (-NMAT .. NN-1). Returns, per step, the rates summed into V0c/V1c[q]."""
+    R = 3 + P
+    C = {}
+    nrel = n - LO
+    c0 = (nrel + 1) // CH if nrel + 1 > 0 else 0
+    # V0c/V1c start as the entering sums (no cell of the pass yet)
+    caps = {st: [list(done.get(st, []))] * (NP // H) for st in (n, n + 1)}
+
+    def cell(step, p, j):
+        assert C[j % R] == j, (LO, n, step, p, j)
+        k = LO + j - n - 1
+        assert -NMAT <= k <= NN - 1
+        rate = LO + p
+        assert k == rate - step - 1
+        done.setdefault(step, []).append(rate)
+
+    c = 0
+    while c * CH < NP:
+        if c >= c0:
+            if c == c0:
+                for j in range(c * CH - 2, c * CH + P):
+                    if j < NP:
+                        C[j % R] = j
+            for p in range(c * CH, min((c + 1) * CH, NP)):
+                if p + P < NP:
+                    C[(p + P) % R] = p + P
+                cell(n, p, p)
+                if p >= 1:
+                    cell(n + 1, p - 1, p - 2)
+                if p % H == H - 1:
+                    caps[n][p // H] = list(done.get(n, []))
+                if p >= 1 and (p - 1) % H == H - 1:
+                    caps[n + 1][(p - 1) // H] = list(done.get(n + 1, []))
+        c += 1
+    cell(n + 1, NP - 1, NP - 2)
+    caps[n + 1][NP // H - 1] = list(done.get(n + 1, []))
+    return caps
+
+
+@pytest.mark.parametrize("ch", [4, 8])
+def test_long_tenor_forward_passes(ch):
+    """k_tpq's forward in two passes of 80 rates at NN=160, NMAT=120: pass 1
+    (rates 0..79) runs the step pairs n < 79, pass 2 (rates 80..159) every
+    pair from pass 1's drift sums at rate 79. Every active cell runs exactly
+    once, each step's cells run up the rates in order (the drift sum's
+    chain), each rate's steps run in order, and the sums saved at the block
+    tops (rates 39, 79, 119, 159) hold exactly the step's active cells at or
+    below the top."""
+    NN, NMAT, H, P = 160, 120, 40, 1
+    HF = 2 * H
+    done = {}
+    saved = {}
+    for n in range(0, NMAT, 2):
+        if n < HF - 1:
+            caps = fwd_pair_pass(HF, H, ch, P, 0, n, NMAT, NN, done)
+        else:
+            caps = {n: [[] for _ in range(HF // H)], n + 1: [[] for _ in range(HF // H)]}
+        for s in (n, n + 1):
+            for q in range(HF // H):
+                saved[(s, q)] = [r for r in caps[s][q] if r > s]
+    for n in range(0, NMAT, 2):
+        caps = fwd_pair_pass(NN - HF, H, ch, P, HF, n, NMAT, NN, done)
+        for s in (n, n + 1):
+            for q in range(2):
+                saved[(s, HF // H + q)] = [r for r in caps[s][q] if r > s]
+    order_by_rate = {}
+    for s in sorted(done):
+        active = [r for r in done[s] if r > s]
+        assert active == sorted(active) and len(set(active)) == len(active), s
+        assert active == list(range(s + 1, NN)), s
+        for r in active:
+            order_by_rate.setdefault(r, []).append(s)
+    for r, steps in order_by_rate.items():
+        assert steps == sorted(steps)
+    for (s, b), rates in saved.items():
+        assert rates == list(range(s + 1, min(b * H + H, NN))), (s, b)
