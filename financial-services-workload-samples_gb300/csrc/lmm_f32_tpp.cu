@@ -1158,8 +1158,10 @@ cudaError_t occ_tps(int *blocks)
 // ---------------------------------------------------------------------------
 // 1: the forward in two passes over 80 rates each (the lower rates for every
 // step, then the upper ones from the drift sums the first pass left at rate
-// 79), so that at most 80 rates are live in registers; 0: all 160 rates in
-// registers. GB300, 1,048,576 paths: 15.69 -> 15.49 ms.
+// 79) through one copy of the pass body, so that at most 80 rates are live
+// in registers; 0: all 160 rates in registers. GB300, 1,048,576 paths,
+// 8-rate chunks: all rates 15.69 ms, two passes written out 15.46, one body
+// 15.20.
 #ifndef LMM_TPQ_FPASS
 #define LMM_TPQ_FPASS 1
 #endif
@@ -1175,7 +1177,12 @@ cudaError_t occ_tps(int *blocks)
 #define LMM_TPQ_FSYNC 0
 #endif
 // Steps per reverse group, reverse and forward chunk lengths and the constant
-// prefetch distance of the long-tenor fused kernel (as LMM_TPP_*).
+// prefetch distance of the long-tenor fused kernel (as LMM_TPP_*). GB300,
+// 1,048,576 paths, the forward in one pass body: forward chunks of 8, 16, 20
+// or 40 rates 15.20, 14.91, 14.97, 15.42 ms; constants one position ahead or
+// at the position of use (16-rate chunks) 14.91, 14.89 ms; two positions
+// ahead 14.99. Groups of 8 steps 18.5 ms (against 15.77 with 4, in an earlier
+// build); reverse chunks of 1, 2, 4 within 1%.
 #ifndef LMM_TPQ_SKEW
 #define LMM_TPQ_SKEW LMM_TPP_SKEW
 #endif
@@ -1186,10 +1193,10 @@ cudaError_t occ_tps(int *blocks)
 #define LMM_TPQ_RCHUNK_PHILOX LMM_TPP_RCHUNK_PHILOX
 #endif
 #ifndef LMM_TPQ_CHUNK
-#define LMM_TPQ_CHUNK LMM_TPP_CHUNK
+#define LMM_TPQ_CHUNK 16
 #endif
 #ifndef LMM_TPQ_PREF
-#define LMM_TPQ_PREF LMM_TPP_PREF
+#define LMM_TPQ_PREF 0
 #endif
 #ifndef LMM_TPQ_PREF_PHILOX
 #define LMM_TPQ_PREF_PHILOX LMM_TPP_PREF_PHILOX
@@ -1426,24 +1433,47 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             unsigned long long mask = 0ull;
 #if LMM_TPQ_FPASS
             {
-                // ---- forward (path_calc_b1 :34-82), pass 1: rates 0 .. HF-1 for every step ----
+                // ---- forward (path_calc_b1 :34-82) in two passes of HF rates through one copy of
+                // the body: pass 0 rates 0 .. HF-1 from the normals, pass 1 rates HF .. NN-1 from
+                // pass 0's drift sums at rate HF-1 ----
                 F2 dprod{1.0f, 0.0f};          // the discount product, rates 0 .. NMAT-1 in order
-                {
-                    float IL[HF];
+                float IL[HF];
+                const float *vin = sc + (size_t)(Lay::s_vt + (HF / H - 1) * NMAT) * B;
+#pragma unroll 1
+                for (int ps = 0; ps < 2; ++ps) {
+                    const int LOp = ps * HF;
 #pragma unroll
-                    for (int i = 0; i < HF; ++i) IL[i] = il0_s[i];
-                    float4 zq, zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
+                    for (int i = 0; i < HF; ++i) IL[i] = il0_s[LOp + i];
+                    float4 zq = make_float4(0.f, 0.f, 0.f, 0.f), zq_next = zq;
+                    float nv0 = 0.0f, nv1 = 0.0f;
+                    if (ps == 0) {
+                        zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
+                    } else {
+                        nv0 = vin[0];
+                        nv1 = vin[B];
+                    }
                     for (int n = 0; n < NMAT; n += 2) {
                         if (LMM_TPQ_FSYNC && (n % (2 * kFsync)) == 0) __syncthreads();
-                        if ((n & 3) == 0) {
-                            zq = zq_next;
-                            if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+                        float V0, V1;
+                        if (ps == 0) {
+                            if ((n & 3) == 0) {
+                                zq = zq_next;
+                                if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
+                            }
+                            V0 = sqd * ((n & 2) ? zq.z : zq.x);     // drift sums from the normal term (kYrun)
+                            V1 = sqd * ((n & 2) ? zq.w : zq.y);
+                        } else {
+                            V0 = nv0;
+                            V1 = nv1;
+                            if (n + 2 < NMAT) {
+                                nv0 = vin[(n + 2) * B];
+                                nv1 = vin[(n + 3) * B];
+                            }
                         }
-                        float V0 = sqd * ((n & 2) ? zq.z : zq.x);     // drift sums from the normal term (kYrun)
-                        float V1 = sqd * ((n & 2) ? zq.w : zq.y);
                         float V0c[HF / H], V1c[HF / H];
-                        if (n < HF - 1) {
-                            fwd_pair_pass<HF, H, LMM_TPQ_CHUNK, PF>(IL, kc0 - (n + 1), delta, n, V0, V1, V0c, V1c);
+                        if (n - LOp < HF - 1) {
+                            fwd_pair_pass<HF, H, LMM_TPQ_CHUNK, PF>(IL, kc0 - (n + 1) + LOp, delta, n - LOp, V0, V1,
+                                                                     V0c, V1c);
                         } else {                 // no rate of the pass moves
 #pragma unroll
                             for (int q = 0; q < HF / H; ++q) {
@@ -1453,57 +1483,26 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                         }
 #pragma unroll
                         for (int q = 0; q < HF / H; ++q) {
-                            sc[(Lay::s_vt + q * NMAT + n) * B] = V0c[q];
-                            sc[(Lay::s_vt + q * NMAT + n + 1) * B] = V1c[q];
+                            sc[(Lay::s_vt + (ps * (HF / H) + q) * NMAT + n) * B] = V0c[q];
+                            sc[(Lay::s_vt + (ps * (HF / H) + q) * NMAT + n + 1) * B] = V1c[q];
                         }
-                        if (nck > 0 && (n + 2) % ckd == 0 && n + 2 < HF - 1) {
+                        if (nck > 0 && (n + 2) % ckd == 0 && n + 2 < NMAT) {
                             // rates i <= n+2 are final from here on: only the others are saved
                             const int c = (n + 2) / ckd - 1;
 #pragma unroll
                             for (int i = 0; i < HF; ++i)
-                                if (i > n + 2) ckp[(c * NN + i) * B] = IL[i];
+                                if (LOp + i > n + 2) ckp[(c * NN + LOp + i) * B] = IL[i];
                         }
                     }
 #pragma unroll
                     for (int i = 0; i < HF; ++i) {
-                        dprod = f2_mul(dprod, bond_ratio(IL[i], delta));
-                        sc[(Lay::s_il + i) * B] = IL[i];
-                    }
-                }
-                // ---- pass 2: rates HF .. NN-1, each step from pass 1's drift sum at rate HF-1 ----
-                float IL[NN - HF];
-#pragma unroll
-                for (int i = 0; i < NN - HF; ++i) IL[i] = il0_s[HF + i];
-                const float *vin = sc + (size_t)(Lay::s_vt + (HF / H - 1) * NMAT) * B;
-                float nv0 = vin[0], nv1 = vin[B];
-                for (int n = 0; n < NMAT; n += 2) {
-                    if (LMM_TPQ_FSYNC && (n % (2 * kFsync)) == 0) __syncthreads();
-                    float V0 = nv0, V1 = nv1;
-                    if (n + 2 < NMAT) {
-                        nv0 = vin[(n + 2) * B];
-                        nv1 = vin[(n + 3) * B];
-                    }
-                    float V0c[(NN - HF) / H], V1c[(NN - HF) / H];
-                    fwd_pair_pass<NN - HF, H, LMM_TPQ_CHUNK, PF>(IL, kc0 - (n + 1) + HF, delta, n - HF, V0, V1, V0c,
-                                                                 V1c);
-#pragma unroll
-                    for (int q = 0; q < (NN - HF) / H; ++q) {
-                        sc[(Lay::s_vt + (HF / H + q) * NMAT + n) * B] = V0c[q];
-                        sc[(Lay::s_vt + (HF / H + q) * NMAT + n + 1) * B] = V1c[q];
-                    }
-                    if (nck > 0 && (n + 2) % ckd == 0 && n + 2 < NMAT) {
-                        const int c = (n + 2) / ckd - 1;
-#pragma unroll
-                        for (int i = 0; i < NN - HF; ++i)
-                            if (HF + i > n + 2) ckp[(c * NN + HF + i) * B] = IL[i];
+                        if (LOp + i < NMAT) {
+                            dprod = f2_mul(dprod, bond_ratio(IL[i], delta));
+                            sc[(Lay::s_il + LOp + i) * B] = IL[i];
+                        }
                     }
                 }
                 // ---- payoff (portfolio_b :133-171, :186-197) and the annuity adjoint ----
-#pragma unroll
-                for (int i = 0; i < NMAT - HF; ++i) {
-                    dprod = f2_mul(dprod, bond_ratio(IL[i], delta));
-                    sc[(Lay::s_il + HF + i) * B] = IL[i];
-                }
                 float *Bst = vg0;
                 float *ILst = vg0 + M * B;
 #pragma unroll

@@ -114,8 +114,10 @@ int lmm_engine_set_stream(lmm_engine *e, void *stream);
  * checkpoints. The default is 8 for every shape but nn = 80, nmat = 40,
  * whose kernel keeps all its drift sums on chip and takes no rate
  * checkpoints (only 0 is accepted there: LMM_ERR_UNSUPPORTED otherwise).
- * nn = 160, nmat = 120 runs its steps in pairs and needs an even interval
- * (LMM_ERR_UNSUPPORTED otherwise); steps outside [0, nmat] is
+ * nn = 160, nmat = 120 restores the checkpoints between groups of four
+ * reverse steps and needs a multiple of 4 (LMM_ERR_UNSUPPORTED otherwise;
+ * its forward/backward pair runs steps in pairs, which any such interval
+ * suits); steps outside [0, nmat] is
  * LMM_ERR_INVALID_ARG. Applies to later calls; a smaller interval may grow
  * the engine's device scratch on the next call. */
 int lmm_engine_set_checkpoint_interval(lmm_engine *e, int32_t steps);
