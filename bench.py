@@ -36,7 +36,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "paths/s value+all Greeks: FP32 adjoint vs FP64 bump, 1 GB300, rel err<=1e-4"
 WORKLOAD = 2
-PROFILE_JSON = os.path.join(ROOT, "profiles", "lmm_fused_f32_80x40.json")
+# The timed fused kernel and its ncu DRAM-traffic summary, per workload that
+# --workload accepts (normals in HBM).
+KERNELS = {2: ("k_tps<80,40,hbm>", os.path.join(ROOT, "profiles", "lmm_fused_f32_80x40.json")),
+           3: ("k_tpq<160,120,hbm>", os.path.join(ROOT, "profiles", "lmm_fused_f32_160x120.json"))}
 
 # Algorithmic operations per path (reference formulas, liborSwaptionGreeks.cpp),
 # counting a divide and an exp as one operation each, C = cells of the
@@ -200,7 +203,7 @@ def run_reference_arm(args):
     if rank != 0:
         return
     cfgm = pkg().configs
-    cfg = cfgm.workload(WORKLOAD)
+    cfg = cfgm.workload(args.workload)
     from oracle import oracle as O
     threads = O.max_threads()
     calib = 65536
@@ -247,7 +250,8 @@ def run_ours(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    cfg = P.configs.workload(WORKLOAD, args.paths)
+    cfg = P.configs.workload(args.workload, args.paths)
+    kernel_name, profile_json = KERNELS[args.workload]
     n, nmat, nout = cfg.paths, cfg.nmat, cfg.nout
     stream = torch.cuda.current_stream(dev)
 
@@ -458,6 +462,8 @@ def run_ours(args):
     if rank == 0 and not args.skip_others:
         others = {}
         for wl, mode in ((3, "hbm"), (4, "philox"), (5, "hbm")):
+            if wl == args.workload:
+                continue
             c = P.configs.workload(wl)
             with P.Engine(c, device=local) as ew:
                 ew.set_stream(stream.cuda_stream)
@@ -489,12 +495,13 @@ def run_ours(args):
         ops = (OPS_PER_CELL * cells(cfg.nn, nmat) + OPS_PORTFOLIO) * n
         peak = P.fp32_peak_tflops(local, 300.0)
         traffic = None
-        if os.path.exists(PROFILE_JSON):
-            with open(PROFILE_JSON) as f:
+        if os.path.exists(profile_json):
+            with open(profile_json) as f:
                 prof = json.load(f)
-            traffic = prof.get("dram_bytes_per_launch")
+            if prof.get("scaled_to_paths") == n:
+                traffic = prof.get("dram_bytes_per_launch")
         achieved = ops / (kms * 1e-3) / 1e12
-        roof = {"bound": "fp32", "kernel": "k_tps<80,40,hbm>", "achieved": achieved,
+        roof = {"bound": "fp32", "kernel": kernel_name, "achieved": achieved,
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "peak_source": "measured live: FFMA-chain kernel lmm_fp32_peak_tflops (MEASURED_PEAKS.json "
                                "has no FP32 SIMT figure)",
@@ -513,8 +520,8 @@ def run_ours(args):
         roof["hbm"] = {"achieved": hbm_ach, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_ach / hbm_peak,
                        "bytes": "ncu DRAM traffic per launch" if traffic else "algorithmic (normals read once)",
                        "peak_source": hbm_src,
-                       "note": "the kernel is not memory-bound: 40 FP32 normals per path against about "
-                               "77k operations"}
+                       "note": f"the kernel is not memory-bound: {nmat} FP32 normals per path against about "
+                               f"{roof['ops_per_path'] / 1e3:.0f}k operations"}
         roof["mufu"] = {"achieved": mach, "peak": mufu["mixed"], "unit": "Gop/s", "frac": mach / mufu["mixed"],
                         "ops_per_path": MUFU_PER_CELL * cells(cfg.nn, nmat) + 2 * cfg.nn,
                         "peak_source": "measured live: lmm_mufu_peak_gops, ex2 and rcp chains alternating",
@@ -552,8 +559,11 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", type=int, default=WORKLOAD, choices=sorted(KERNELS),
+                    help="the workload timed as the bench line: 2 = 80/40 at 4,194,304 paths (default), "
+                         "3 = 160/120 at 1,048,576 paths with rates saved every 8 steps")
     ap.add_argument("--paths", type=int, default=None,
-                    help="paths per step (default: the workload's 4,194,304); smaller only for profiling")
+                    help="paths per step (default: the workload's own count); smaller only for profiling")
     ap.add_argument("--bump-paths", type=int, default=16384)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--kernel-times", action="store_true",
