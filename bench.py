@@ -374,12 +374,16 @@ def run_ours(args):
         fw = med_ms(lambda: eng.forward_f32_device(dz.data_ptr(), n, tape, val.data_ptr()))
         bw = med_ms(lambda: eng.backward_f32_device(dz.data_ptr(), tape, [1.0], grad.data_ptr()))
         tape.close()
+        long_tenor = cfg.nn == 160
         phases = {"forward_ms": fw, "backward_ms": bw, "fused_ms": statistics.median(kern_ms),
-                  "tape_bytes": 4 * (cfg.nn + nmat) * n,
+                  "tape_bytes": 4 * (cfg.nn + (2 if long_tenor else 1) * nmat) * n,
                   "note": "forward = Euler steps + payoff + tape write (terminal rates, per-step drift "
-                          "sums); backward = tape read + payoff adjoint + reverse sweep (the pair runs "
-                          "the one-pass k_tpp kernels); the fused call keeps its state on chip, the "
-                          "idle rate half in an L2 scratch"}
+                          "sums" + (", and the drift sums at rate 79" if long_tenor else "") +
+                          "); backward = tape read + payoff adjoint + reverse sweep (the pair runs " +
+                          ("the two-thread k_tp2 kernels; the fused call runs k_tpq, one thread per path "
+                           "in 40-rate blocks with a per-block scratch" if long_tenor else
+                           "the one-pass k_tpp kernels; the fused call keeps its state on chip, the "
+                           "idle rate half in an L2 scratch") + ")"}
 
     # ---- the MRG32k3a/AS241 normal stream (the reference's generator family):
     # the workload's normals generated on the device vs the oracle on one core
