@@ -25,9 +25,10 @@ def P():
     return pkg()
 
 
-@pytest.mark.parametrize("k", [0, 4, 8, 16])
+@pytest.mark.parametrize("k", [0, 4, 8, 12, 16, 116])
 def test_long_tenor_interval_matches_oracle(P, k):
-    """160x120 (two threads per path), 30 swaptions, random curve and vols:
+    """160x120 (the fused call: one thread per path in 40-rate block passes),
+    30 swaptions, random curve and vols:
     rates restored every k steps (0: never), on the same normals for every k
     (those of test_long_tenor_checkpointed_fp32_matches_oracle)."""
     cfg = cfgs().workload(3, 512)
@@ -71,9 +72,9 @@ def test_interval_changes_only_rounding(P):
 
 def test_interval_errors(P):
     """80/40 keeps every drift sum on chip and takes no rate checkpoints; the
-    160/120 kernels restore checkpoints between step pairs or groups of four
-    (odd k is refused either way); k must lie in [0, nmat]. A refused setting
-    leaves the interval as it was."""
+    160/120 fused kernel restores checkpoints between groups of four reverse
+    steps (k not a multiple of 4 is refused); k must lie in [0, nmat]. A
+    refused setting leaves the interval as it was."""
     with P.Engine(cfgs().workload(2, 64)) as e:
         assert e.checkpoint_interval == 0
         e.set_checkpoint_interval(0)
@@ -82,7 +83,7 @@ def test_interval_errors(P):
         assert ei.value.code == -2
         assert e.checkpoint_interval == 0
     with P.Engine(cfgs().workload(3, 64)) as e:
-        for bad, code in ((3, -2), (-1, -1), (121, -1)):
+        for bad, code in ((3, -2), (6, -2), (-1, -1), (121, -1)):
             with pytest.raises(P.LmmError) as ei:
                 e.set_checkpoint_interval(bad)
             assert ei.value.code == code

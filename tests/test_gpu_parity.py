@@ -261,9 +261,10 @@ def _random_cfg(nn, nmat, nopt, seed, paths, vol=(0.1, 0.2)):
 
 @pytest.mark.parametrize("philox", [False, True])
 def test_long_tenor_checkpointed_fp32_matches_oracle(P, philox):
-    """Workload 3 (NN=160, NMAT=120, 30 swaptions): the two-threads-per-path
-    kernel, whose reverse sweep rebuilds each step from the forward's drift
-    sums at both half tops and takes the rates saved every 8 steps."""
+    """Workload 3 (NN=160, NMAT=120, 30 swaptions): the fused call runs one
+    thread per path, the forward in two passes of 80 rates and the reverse in
+    passes over blocks of 40 rates, each step rebuilt from the forward's drift
+    sum at the block's top rate, with the rates saved every 8 steps."""
     cfg = cfgs().workload(3, 512)
     seed = 303
     z = O.normals_f32(seed, cfg.paths, cfg.nmat)
@@ -288,8 +289,9 @@ def test_other_shapes_fp32_match_oracle(P, nn, nmat, nopt):
 
 @pytest.mark.parametrize("shape", [(160, 120, 3), (33, 7, 2), (200, 100, 4)])
 def test_pair_api_on_other_shapes(P, shape):
-    """160x120 (two threads per path, tape of terminal rates and drift sums)
-    and the warp-per-path shapes (the backward recomputes the forward from the
+    """160x120 (the pair runs two threads per path with a tape of terminal
+    rates and drift sums; the fused call one thread per path) and the
+    warp-per-path shapes (the backward recomputes the forward from the
     same normals): value and vbar-scaled Greeks equal the fused call's."""
     import torch
     nn, nmat, seed = shape
@@ -471,11 +473,12 @@ def test_pipelined_host_call_equals_device_call(P, paths):
 
 
 @pytest.mark.parametrize("paths,nscen", [(1, 1), (77, 1), (300, 2)])
-def test_two_threads_per_path_ragged_and_scenarios(P, paths, nscen):
-    """160x120 runs two threads per path in batches of 128 paths: a ragged
-    last batch leaves lanes of both halves idle, and scenarios loop over units
-    of the one-block-per-SM grid. Every scenario matches the FP64 oracle, and
-    the forward/backward pair equals the fused call."""
+def test_long_tenor_ragged_and_scenarios(P, paths, nscen):
+    """160x120: the fused call runs one thread per path in batches of 256
+    paths, the forward/backward pair two threads per path in batches of 128;
+    a ragged last batch leaves lanes idle, and scenarios loop over units of
+    the one-block-per-SM grid. Every scenario matches the FP64 oracle, and the
+    pair equals the fused call to FP32 rounding."""
     import torch
     base = cfgs().workload(3, paths)
     cfg = base.with_paths(paths)
