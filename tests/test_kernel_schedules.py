@@ -536,3 +536,66 @@ def test_long_tenor_forward_passes(ch):
         assert steps == sorted(steps)
     for (s, b), rates in saved.items():
         assert rates == list(range(s + 1, min(b * H + H, NN))), (s, b)
+
+
+def fwd_pair_rcp2(NN, CH, n):
+    """Replays fwd_pair_window_cap with LMM_FWD_RCP2 (csrc/lmm_f32_tpp.cu):
+    steps n, n+1 over NN rates; returns, per cell (step, rate), the
+    reciprocal pair it took its 1/(IL + delta) from, as ((rate a, version of
+    a), (rate b, version of b), which), a version being the number of cells
+    run on the rate before. Every cell must take the reciprocal of its own
+    rate's current value."""
+    ver = [0] * NN
+    used = {}
+    c0 = (n + 1) // CH
+    t0n = t1n = None
+
+    def pair(a, b):
+        pr = ((a, ver[a]), (b, ver[b]))
+        return (pr, 0), (pr, 1)
+
+    def cell(step, i, t):
+        (pr, which) = t
+        assert pr[which] == (i, ver[i]), (n, step, i, pr, which, ver[i])
+        used[(step, i)] = t
+        ver[i] += 1
+
+    c = 0
+    while c * CH < NN:
+        if c >= c0:
+            if c == c0 and c * CH >= 2:
+                _, t1n = pair(c * CH - 2, c * CH - 1)
+            for p in range(c * CH, min((c + 1) * CH, NN)):
+                if p % 2 == 0:
+                    t, t0n = pair(p, p + 1)
+                else:
+                    t = t0n
+                if p >= 1:
+                    cell(n, p, t)
+                if p % 2 == 1:
+                    ta, t1n = pair(p - 1, p)
+                    if p - 1 >= 1:
+                        cell(n + 1, p - 1, ta)
+                elif p - 1 >= 1:
+                    cell(n + 1, p - 1, t1n)
+        c += 1
+    cell(n + 1, NN - 1, t1n)
+    return used
+
+
+@pytest.mark.parametrize("ch", [2, 4, 8, 16])
+def test_forward_reciprocal_pairs(ch):
+    """With LMM_FWD_RCP2 the fused forward's skewed step pairs and the
+    forward-only kernel's single steps (fwd_step_chunked) share each MUFU
+    reciprocal between the cells of one step at positions 2m and 2m+1, in
+    the same argument order: every cell takes the reciprocal of its own
+    rate's value at the cell, and both kernels form the same pairs, so they
+    round alike (the forward/backward pair reproduces the fused value)."""
+    NN = 80
+    for n in range(0, 40, 2):
+        used = fwd_pair_rcp2(NN, ch, n)
+        for step in (n, n + 1):
+            c0 = (step + 1) // ch
+            for i in range(max(1, c0 * ch), NN):
+                (pr, which) = used[(step, i)]
+                assert pr[0][0] == i - i % 2 and pr[1][0] == i - i % 2 + 1 and which == i % 2, (step, i, pr)
