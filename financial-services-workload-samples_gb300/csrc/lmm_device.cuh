@@ -15,6 +15,17 @@
 #define LMM_COMP_SUMS 1
 #endif
 
+// 1: the long-tenor (160/120) forwards share one MUFU reciprocal between the
+// cells of one step at rates 2m and 2m+1 (rcp_pair), as the 80/40 forwards do
+// with LMM_FWD_RCP2. Shared by the fused kernel (lmm_f32_tpp.cu) and the
+// thread pair of the forward/backward API (lmm_f32_tp2.cu), which must round
+// alike. GB300, fused 160/120 kernel at 1,048,576 paths: 14.19 ms without,
+// 18.8 ms with (its 255-register forward pass does not take the pairs'
+// extra live values), so it is off.
+#ifndef LMM_FWD_RCP2_LONG
+#define LMM_FWD_RCP2_LONG 0
+#endif
+
 namespace lmm {
 
 // MUFU approximations issued directly (PTX ISA: rcp.approx.ftz.f32,
@@ -31,6 +42,15 @@ __device__ __forceinline__ float ex2_approx(float x)
     float r;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
+}
+
+// Two reciprocals from one: 1/a = b/(ab), 1/b = a/(ab) (the forward's a, b =
+// 1/L + delta lie in [delta, 1e4]: ab stays far inside FP32 range).
+__device__ __forceinline__ void rcp_pair(float a, float b, float &ta, float &tb)
+{
+    const float r = rcp_approx(a * b);
+    ta = b * r;
+    tb = a * r;
 }
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): multipliers 0xD2511F53,

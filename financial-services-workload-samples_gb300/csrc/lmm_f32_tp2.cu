@@ -139,6 +139,13 @@ __device__ __forceinline__ void tp2_fwd_cell(float &X, float &Y, const float4 &k
     X *= ex2_approx(-fmaf(k.x, Y, k.y));
 }
 
+// tp2_fwd_cell with t = 1/(X + delta) given.
+__device__ __forceinline__ void tp2_fwd_cell_t(float &X, float &Y, const float4 &k, float t)
+{
+    Y = fmaf(k.z, t, Y);
+    X *= ex2_approx(-fmaf(k.x, Y, k.y));
+}
+
 // Steps n and n+1 over one block of L rates held in X[OFF .. OFF+L) (local
 // position p, the block's rate p): cell (n, p) and cell (n+1, p-1) at
 // position p; kcn[j] holds the constants of step n at the block's rate j,
@@ -151,6 +158,11 @@ __device__ __forceinline__ void tp2_fwd_pair(float (&X)[NX], const float4 *kcn, 
 {
     constexpr int R = 3 + P;
     float4 C[R];
+    // LMM_FWD_RCP2_LONG: the cells of one step at rates 2m, 2m+1 share one
+    // reciprocal, paired and ordered as in the fused kernel (the block's first
+    // rate is even), so the two round alike
+    static_assert(!LMM_FWD_RCP2_LONG || (CH % 2 == 0 && L % 2 == 0), "reciprocal pairs (2m, 2m+1) inside chunks");
+    float t0n = 0.0f, t1n = 0.0f;
 #pragma unroll
     for (int c = 0; c * CH < L; ++c) {
         if (c >= c0) {
@@ -158,16 +170,39 @@ __device__ __forceinline__ void tp2_fwd_pair(float (&X)[NX], const float4 *kcn, 
 #pragma unroll
                 for (int j = c * CH - 2; j < c * CH + P; ++j)
                     if (j < L) C[(j + R) % R] = kcn[j];
+                if (LMM_FWD_RCP2_LONG && c * CH >= 2) {       // step n+1's pair below the chunk
+                    float ta;
+                    rcp_pair(X[OFF + c * CH - 2] + delta, X[OFF + c * CH - 1] + delta, ta, t1n);
+                }
             }
 #pragma unroll
             for (int p = c * CH; p < (c + 1) * CH && p < L; ++p) {
                 if (p + P < L) C[(p + P) % R] = kcn[p + P];
-                tp2_fwd_cell(X[OFF + p], Y0, C[p % R], delta);
-                if (p >= 1) tp2_fwd_cell(X[OFF + p - 1], Y1, C[(p + R - 2) % R], delta);
+                if (LMM_FWD_RCP2_LONG) {
+                    float t;
+                    if (p % 2 == 0)
+                        rcp_pair(X[OFF + p] + delta, X[OFF + p + 1] + delta, t, t0n);
+                    else
+                        t = t0n;
+                    tp2_fwd_cell_t(X[OFF + p], Y0, C[p % R], t);
+                    if (p % 2 == 1) {
+                        float ta;
+                        rcp_pair(X[OFF + p - 1] + delta, X[OFF + p] + delta, ta, t1n);
+                        tp2_fwd_cell_t(X[OFF + p - 1], Y1, C[(p + R - 2) % R], ta);
+                    } else if (p >= 1) {
+                        tp2_fwd_cell_t(X[OFF + p - 1], Y1, C[(p + R - 2) % R], t1n);
+                    }
+                } else {
+                    tp2_fwd_cell(X[OFF + p], Y0, C[p % R], delta);
+                    if (p >= 1) tp2_fwd_cell(X[OFF + p - 1], Y1, C[(p + R - 2) % R], delta);
+                }
             }
         }
     }
-    tp2_fwd_cell(X[OFF + L - 1], Y1, C[(L - 2) % R], delta);
+    if (LMM_FWD_RCP2_LONG)
+        tp2_fwd_cell_t(X[OFF + L - 1], Y1, C[(L - 2) % R], t1n);
+    else
+        tp2_fwd_cell(X[OFF + L - 1], Y1, C[(L - 2) % R], delta);
 }
 
 // Reverse cell (path_calc_b2 :105-111 in log-adjoint form) + vega on one

@@ -223,15 +223,6 @@ __device__ __forceinline__ void fwd_cell_t(float &IL, float &V, const float4 &k,
     IL *= ex2_approx(-fmaf(k.x, kYrun ? V : V + sqez, k.y));
 }
 
-// Two reciprocals from one: 1/a = b/(ab), 1/b = a/(ab) (a, b in [delta, 1e4]:
-// ab stays far inside FP32 range).
-__device__ __forceinline__ void rcp_pair(float a, float b, float &ta, float &tb)
-{
-    const float r = rcp_approx(a * b);
-    ta = b * r;
-    tb = a * r;
-}
-
 // 1: the forward cells of one step at positions 2m and 2m+1 share one MUFU
 // reciprocal (rcp_pair), in the 80/40 forwards (the fused kernels' skewed
 // pairs and the forward-only kernel's single steps). The forward runs two
@@ -1208,15 +1199,6 @@ cudaError_t occ_tps(int *blocks)
 // [NN-H] parked inverse rates of the lower blocks, [NN-H] deltas of the upper
 // blocks, [NCK][NN] rate checkpoints.
 // ---------------------------------------------------------------------------
-// 1: the forward in two passes over 80 rates each (the lower rates for every
-// step, then the upper ones from the drift sums the first pass left at rate
-// 79) through one copy of the pass body, so that at most 80 rates are live
-// in registers; 0: all 160 rates in registers. GB300, 1,048,576 paths,
-// 8-rate chunks: all rates 15.69 ms, two passes written out 15.46, one body
-// 15.20.
-#ifndef LMM_TPQ_FPASS
-#define LMM_TPQ_FPASS 1
-#endif
 #ifndef LMM_TPQ_BLOCK
 #define LMM_TPQ_BLOCK 256
 #endif
@@ -1287,44 +1269,6 @@ struct TpqLayout {
     static_assert(NN % H == 0 && M == H && H % 4 == 0, "the top block is the annuity rates");
 };
 
-// Forward steps n and n+1 as fwd_pair_window, also returning the drift sums
-// of both steps at the top rate of every H-rate block but the last.
-template <int NN, int H, int CH, int P>
-__device__ __forceinline__ void fwd_pair_window_caps(float (&IL)[NN], const float4 *kcn, float sqez0,
-                                                     float sqez1, float delta, int n, float &V0, float &V1,
-                                                     float (&V0c)[NN / H - 1], float (&V1c)[NN / H - 1])
-{
-    constexpr int R = 3 + P;
-    float4 C[R];
-    V0 = drift0(sqez0);
-    V1 = drift0(sqez1);
-#pragma unroll
-    for (int b = 0; b < NN / H - 1; ++b) {
-        V0c[b] = V0;
-        V1c[b] = V1;
-    }
-    const int c0 = (n + 1) / CH;
-#pragma unroll
-    for (int c = 0; c * CH < NN; ++c) {
-        if (c >= c0) {
-            if (c == c0) {
-#pragma unroll
-                for (int j = c * CH - 2; j < c * CH + P; ++j)
-                    if (j >= 0 && j < NN) C[j % R] = kcn[j];
-            }
-#pragma unroll
-            for (int p = c * CH; p < (c + 1) * CH && p < NN; ++p) {
-                if (p + P < NN) C[(p + P) % R] = kcn[p + P];
-                if (p >= 1) fwd_cell(IL[p], V0, C[p % R], sqez0, delta);
-                if (p - 1 >= 1) fwd_cell(IL[p - 1], V1, C[(p + R - 2) % R], sqez1, delta);
-                if (p % H == H - 1 && p < NN - 1) V0c[p / H] = V0;
-                if (p >= 1 && (p - 1) % H == H - 1 && p - 1 < NN - 1) V1c[(p - 1) / H] = V1;
-            }
-        }
-    }
-    fwd_cell(IL[NN - 1], V1, C[(NN - 2) % R], sqez1, delta);
-}
-
 // Forward steps n and n+1 over the NP rates LO .. LO+NP-1 held in IL[] at
 // local positions 0 .. NP-1, paired as fwd_pair_window: cell (n, p) with
 // cell (n+1, p-1). V0, V1 enter as the steps' drift sums below the pass (at
@@ -1345,6 +1289,8 @@ __device__ __forceinline__ void fwd_pair_pass(float (&IL)[NP], const float4 *kcn
         V1c[q] = V1;
     }
     const int c0 = nrel + 1 > 0 ? (nrel + 1) / CH : 0;
+    static_assert(!LMM_FWD_RCP2_LONG || (CH % 2 == 0 && NP % 2 == 0), "reciprocal pairs (2m, 2m+1) inside chunks");
+    float t0n = 0.0f, t1n = 0.0f;   // LMM_FWD_RCP2_LONG: the second reciprocals of the steps' pairs in flight
 #pragma unroll
     for (int c = 0; c * CH < NP; ++c) {
         if (c >= c0) {
@@ -1352,18 +1298,42 @@ __device__ __forceinline__ void fwd_pair_pass(float (&IL)[NP], const float4 *kcn
 #pragma unroll
                 for (int j = c * CH - 2; j < c * CH + P; ++j)
                     if (j < NP) C[(j % R + R) % R] = kcn[j];
+                // step n+1's pair below the chunk: rates inactive in step n, unchanged
+                if (LMM_FWD_RCP2_LONG && c * CH >= 2) {
+                    float ta;
+                    rcp_pair(IL[c * CH - 2] + delta, IL[c * CH - 1] + delta, ta, t1n);
+                }
             }
 #pragma unroll
             for (int p = c * CH; p < (c + 1) * CH && p < NP; ++p) {
                 if (p + P < NP) C[(p + P) % R] = kcn[p + P];
-                fwd_cell(IL[p], V0, C[p % R], 0.0f, delta);
-                if (p >= 1) fwd_cell(IL[p - 1], V1, C[((p - 2) % R + R) % R], 0.0f, delta);
+                if (LMM_FWD_RCP2_LONG) {     // pairs as fwd_pair_window_cap (LO even)
+                    float t;
+                    if (p % 2 == 0)
+                        rcp_pair(IL[p] + delta, IL[p + 1] + delta, t, t0n);
+                    else
+                        t = t0n;
+                    fwd_cell_t(IL[p], V0, C[p % R], 0.0f, t);
+                    if (p % 2 == 1) {
+                        float ta;
+                        rcp_pair(IL[p - 1] + delta, IL[p] + delta, ta, t1n);
+                        fwd_cell_t(IL[p - 1], V1, C[((p - 2) % R + R) % R], 0.0f, ta);
+                    } else if (p >= 1) {
+                        fwd_cell_t(IL[p - 1], V1, C[((p - 2) % R + R) % R], 0.0f, t1n);
+                    }
+                } else {
+                    fwd_cell(IL[p], V0, C[p % R], 0.0f, delta);
+                    if (p >= 1) fwd_cell(IL[p - 1], V1, C[((p - 2) % R + R) % R], 0.0f, delta);
+                }
                 if (p % H == H - 1) V0c[p / H] = V0;
                 if (p >= 1 && (p - 1) % H == H - 1) V1c[(p - 1) / H] = V1;
             }
         }
     }
-    fwd_cell(IL[NP - 1], V1, C[(NP - 2) % R], 0.0f, delta);
+    if (LMM_FWD_RCP2_LONG)
+        fwd_cell_t(IL[NP - 1], V1, C[(NP - 2) % R], 0.0f, t1n);
+    else
+        fwd_cell(IL[NP - 1], V1, C[(NP - 2) % R], 0.0f, delta);
     V1c[NP / H - 1] = V1;
 }
 
@@ -1440,9 +1410,9 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
     static_assert(NMAT % 4 == 0 && NMAT % G == 0 && H % G == 0, "normals in quads, reverse steps in groups");
     static_assert(RCH - 1 <= Lay::VPAD, "the windows' spare vega rows lie inside the table");
     constexpr int kFsync = LMM_TPQ_FSYNC > 0 ? LMM_TPQ_FSYNC : 1, kRsync = LMM_TPQ_RSYNC > 0 ? LMM_TPQ_RSYNC : 1;
-    constexpr int HF = 2 * H;      // rates per forward pass (LMM_TPQ_FPASS)
+    constexpr int HF = 2 * H;      // rates per forward pass
     static_assert(kYrun, "the drift sums carry the normal term");
-    static_assert(!LMM_TPQ_FPASS || (NN == 2 * HF && NMAT > HF && NMAT - HF + M == HF), "two forward passes");
+    static_assert(NN == 2 * HF && NMAT > HF && NMAT - HF + M == HF, "two forward passes");
     extern __shared__ __align__(16) unsigned char smem[];
     float *il0_s = reinterpret_cast<float *>(smem + Lay::il0);
     int *ost_s = reinterpret_cast<int *>(smem + Lay::ost);
@@ -1495,7 +1465,6 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
             float disc = 1.0f, V, vs;
             float X[H], Pb[H];        // the block in the reverse: inverse rates, log-adjoints
             unsigned long long mask = 0ull;
-#if LMM_TPQ_FPASS
             {
                 // ---- forward (path_calc_b1 :34-82) in two passes of HF rates through one copy of
                 // the body: pass 0 rates 0 .. HF-1 from the normals, pass 1 rates HF .. NN-1 from
@@ -1580,54 +1549,6 @@ k_tpq(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 }
                 vs = -V * delta;
             }
-#else
-            {
-                // ---- forward over all NN rates (path_calc_b1 :34-82) ----
-                float IL[NN];
-#pragma unroll
-                for (int i = 0; i < NN; ++i) IL[i] = il0_s[i];
-                float4 zq, zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
-                for (int n = 0; n < NMAT; n += 2) {
-                    if (LMM_TPQ_FSYNC && (n % (2 * kFsync)) == 0) __syncthreads();
-                    if ((n & 3) == 0) {
-                        zq = zq_next;
-                        if ((n >> 2) + 1 < NMAT / 4) zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, (n >> 2) + 1);
-                    }
-                    const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
-                    const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
-                    float V0, V1, V0c[Q - 1], V1c[Q - 1];
-                    fwd_pair_window_caps<NN, H, LMM_TPQ_CHUNK, PF>(IL, kc0 - (n + 1), sqez0, sqez1, delta,
-                                                                             n, V0, V1, V0c, V1c);
-#pragma unroll
-                    for (int b = 0; b < Q - 1; ++b) {
-                        sc[(Lay::s_vt + b * NMAT + n) * B] = V0c[b];
-                        sc[(Lay::s_vt + b * NMAT + n + 1) * B] = V1c[b];
-                    }
-                    sc[(Lay::s_vt + (Q - 1) * NMAT + n) * B] = V0;
-                    sc[(Lay::s_vt + (Q - 1) * NMAT + n + 1) * B] = V1;
-                    if (nck > 0 && (n + 2) % ckd == 0 && n + 2 < NMAT) {
-                        // rates i <= n+2 are final from here on: only the others are saved
-                        const int c = (n + 2) / ckd - 1;
-#pragma unroll
-                        for (int i = 0; i < NN; ++i)
-                            if (i > n + 2) ckp[(c * NN + i) * B] = IL[i];
-                    }
-                }
-                // ---- payoff (portfolio_b :133-171, :186-197) and the annuity adjoint ----
-                float *Bst = vg0;
-                float *ILst = vg0 + M * B;
-                V = payoff_forward<NN, NMAT, B>(IL, delta, ost_s, okk_s, owf_s, &disc, Bst, ILst, &mask);
-                payoff_adjoint_stage<NN, NMAT, B>(1.0f, disc, Bst, ILst, mask, delta, ost_s, okf_s, owf_s);
-#pragma unroll
-                for (int i = 0; i < H; ++i) {
-                    X[i] = IL[NN - H + i];
-                    Pb[i] = ILst[i * B];
-                }
-#pragma unroll
-                for (int i = 0; i < NN - H; ++i) sc[(Lay::s_il + i) * B] = IL[i];
-                vs = -V * delta;
-            }
-#endif
 #pragma unroll
             for (int k = 0; k < NN; ++k) vg0[k * B] = 0.0f;
 

@@ -538,7 +538,7 @@ def test_long_tenor_forward_passes(ch):
         assert rates == list(range(s + 1, min(b * H + H, NN))), (s, b)
 
 
-def fwd_pair_rcp2(NN, CH, n):
+def fwd_pair_rcp2(NN, CH, n, first=1):
     """Replays fwd_pair_window_cap with LMM_FWD_RCP2 (csrc/lmm_f32_tpp.cu):
     steps n, n+1 over NN rates; returns, per cell (step, rate), the
     reciprocal pair it took its 1/(IL + delta) from, as ((rate a, version of
@@ -547,7 +547,7 @@ def fwd_pair_rcp2(NN, CH, n):
     rate's current value."""
     ver = [0] * NN
     used = {}
-    c0 = (n + 1) // CH
+    c0 = (n + 1) // CH if n + 1 > 0 else 0
     t0n = t1n = None
 
     def pair(a, b):
@@ -570,13 +570,13 @@ def fwd_pair_rcp2(NN, CH, n):
                     t, t0n = pair(p, p + 1)
                 else:
                     t = t0n
-                if p >= 1:
+                if p >= first:
                     cell(n, p, t)
                 if p % 2 == 1:
                     ta, t1n = pair(p - 1, p)
-                    if p - 1 >= 1:
+                    if p - 1 >= first:
                         cell(n + 1, p - 1, ta)
-                elif p - 1 >= 1:
+                elif p - 1 >= first:
                     cell(n + 1, p - 1, t1n)
         c += 1
     cell(n + 1, NN - 1, t1n)
@@ -599,3 +599,21 @@ def test_forward_reciprocal_pairs(ch):
             for i in range(max(1, c0 * ch), NN):
                 (pr, which) = used[(step, i)]
                 assert pr[0][0] == i - i % 2 and pr[1][0] == i - i % 2 + 1 and which == i % 2, (step, i, pr)
+
+
+@pytest.mark.parametrize("ch", [2, 4, 16])
+def test_long_tenor_forward_reciprocal_pairs(ch):
+    """LMM_FWD_RCP2_LONG in k_tpq's forward passes (fwd_pair_pass, every cell
+    of the pass runs, from local position 0) and in the thread pair's blocks
+    (tp2_fwd_pair, the same body): each cell takes the reciprocal of its own
+    rate's current value, from the pair of local positions (2m, 2m+1); the
+    passes and blocks start at even rates (0, 40, 80, 120), so both kernels
+    pair the global rates (2m, 2m+1) alike."""
+    for NP, LO in ((80, 0), (80, 80), (40, 40)):
+        assert LO % 2 == 0
+        for n in range(0, 120, 2):
+            if n - LO >= NP - 1:
+                continue
+            used = fwd_pair_rcp2(NP, ch, n - LO, first=0)
+            for (step, i), (pr, which) in used.items():
+                assert pr[0][0] == i - i % 2 and pr[1][0] == i - i % 2 + 1 and which == i % 2
