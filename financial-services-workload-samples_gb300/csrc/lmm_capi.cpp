@@ -187,17 +187,19 @@ int f32_family(const lmm_engine *e)
     return 0;
 }
 
-// Kernel family of an FP32 call: 5 (two threads per path, lmm_f32_tp2.cu)
-// for nn=160, nmat=120, every mode; 6 (one thread per path with the reverse
-// split over the rate halves, k_tps) for fused 80/40 calls (LMM_USE_TPS);
-// otherwise f32_family. On GB300 at 160/120 the thread pair runs 2.1x the
-// warp-per-path rate; at 80/40 it ran 13.4-15.5 ms against 11.7 ms for the
-// thread-per-path kernel (4,194,304 paths), so it does not take that shape.
+// Kernel family of an FP32 call: 7 (one thread per path, the forward in two
+// passes of 80 rates and the reverse in passes over blocks of 40 rates,
+// k_tpq) for fused nn=160, nmat=120 calls (LMM_USE_TPQ; GB300, 1,048,576
+// paths: 14.15 ms against 18.29 for the thread pair); 5 (two threads per
+// path, lmm_f32_tp2.cu) for that shape's forward/backward pair (and its fused
+// calls without LMM_USE_TPQ; 2.1x the warp-per-path rate); 6 (one thread per
+// path with the reverse split over the rate halves, k_tps) for fused 80/40
+// calls (LMM_USE_TPS); otherwise f32_family. At 80/40 the thread pair ran
+// 13.4-15.5 ms against 11.7 ms for the thread-per-path kernel (4,194,304
+// paths), so it does not take that shape.
 #ifndef LMM_USE_TPS
 #define LMM_USE_TPS 1
 #endif
-// 7 (one thread per path, the reverse in passes over blocks of 40 rates,
-// k_tpq) for fused 160/120 calls (LMM_USE_TPQ); the pair keeps family 5.
 #ifndef LMM_USE_TPQ
 #define LMM_USE_TPQ 1
 #endif
