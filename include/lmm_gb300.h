@@ -273,7 +273,8 @@ int lmm_mrg32k3a_normals_f32_device(uint32_t seed, int64_t first, int64_t count,
  * and without any allocation (no cudaMalloc, no cudaFree, no allocating
  * library call). It runs the one-pass kernel, which needs no per-path
  * scratch; the engine's fused call runs the split-reverse kernel, and the
- * two agree within the FP32 tolerance (same cells, rounded in another order). The caller passes the parameters, the device normals d_z and the
+ * two agree within the FP32 tolerance (same cells, rounded in another
+ * order). The caller passes the parameters, the device normals d_z and the
  * device outputs d_out/d_se (layout as above); everything else -- model
  * constants, per-block partial sums, the non-finite flag -- lives in one
  * static device array of LMM_NOALLOC_SCRATCH_BYTES that every GPU loading
@@ -285,7 +286,9 @@ int lmm_mrg32k3a_normals_f32_device(uint32_t seed, int64_t first, int64_t count,
  *     caller's host memory is read after the call returns.
  *   - The first call on a device looks up the array's device address and the
  *     kernel's occupancy and caches them: make it before any stream capture.
- *     After cudaDeviceReset the next call on that device looks them up again.
+ *     Later calls enqueue only kernels, so a stream capture records them and
+ *     graph replays repeat the call (tested). After cudaDeviceReset the next
+ *     call on that device looks them up again.
  *   - Every call shares the one array, which keeps the last call's
  *     contents: calls that overlap on the GPU (other streams, other host
  *     threads) race on it and must be serialised by the caller.

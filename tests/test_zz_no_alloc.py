@@ -89,3 +89,34 @@ def test_noalloc_limits_are_errors():
     one = cfgs().workload(1, 64)
     assert _call(P, one, dz, 0, out, se, 0) == -1
     assert "paths" in P.last_error()
+
+
+def test_noalloc_replays_from_a_cuda_graph():
+    """After a first call outside any capture (which looks up the static
+    scratch and the occupancy), the call enqueues only kernels on the given
+    stream -- the model constants travel as a kernel's parameters, not as a
+    copy from host memory -- so a stream capture records it, and replays,
+    with the host's parameter struct gone, return the direct call's bits."""
+    import torch
+    P = pkg()
+    cfg = cfgs().workload(2, 40_000)
+    n = cfg.paths
+    dz = torch.empty(n * cfg.nmat, dtype=torch.float32, device="cuda")
+    P.normals_f32_device(31, n, cfg.nmat, dz.data_ptr())
+    out_d = torch.zeros(cfg.nout, dtype=torch.float64, device="cuda")
+    se_d = torch.zeros_like(out_d)
+    out_g = torch.zeros_like(out_d)
+    se_g = torch.zeros_like(out_d)
+    s = torch.cuda.Stream()
+    assert _call(P, cfg, dz, n, out_d, se_d, s.cuda_stream) == 0
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        assert _call(P, cfg, dz, n, out_g, se_g, s.cuda_stream) == 0
+    for _ in range(3):
+        out_g.zero_()
+        se_g.zero_()
+        g.replay()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out_g.cpu().numpy(), out_d.cpu().numpy())
+    np.testing.assert_array_equal(se_g.cpu().numpy(), se_d.cpu().numpy())
