@@ -880,6 +880,34 @@ k_tpp(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 #ifndef LMM_TPS_KCPARAM
 #define LMM_TPS_KCPARAM 1
 #endif
+// Forward step pairs between block barriers, reverse chunk lengths and the
+// constant prefetch distance of k_tps, with normals from memory and with
+// Philox normals (the k_tpp kernels keep LMM_TPP_*). GB300, with the shared
+// forward reciprocals: 4,194,304 paths, a forward barrier every 2, 4, 8 pairs
+// or once per batch (20 pairs) 10.01, 9.88, 9.86, 9.83 ms; constants at the
+// position of use 9.98 against 9.88 (one ahead); 16.8M Philox paths, 42.35 ms
+// as LMM_TPP_*, 41.54 with 2-position reverse chunks and constants one ahead,
+// 41.33 / 41.24 / 41.15 / 40.81 with a forward barrier every 2 / 4 / 8 pairs /
+// once per batch. 256 curves x 262,144 paths with these settings: 163.5 ms
+// (166.2 before).
+#ifndef LMM_TPS_FSYNC
+#define LMM_TPS_FSYNC 20
+#endif
+#ifndef LMM_TPS_FSYNC_PHILOX
+#define LMM_TPS_FSYNC_PHILOX 20
+#endif
+#ifndef LMM_TPS_RCHUNK
+#define LMM_TPS_RCHUNK LMM_TPP_RCHUNK
+#endif
+#ifndef LMM_TPS_RCHUNK_PHILOX
+#define LMM_TPS_RCHUNK_PHILOX 2
+#endif
+#ifndef LMM_TPS_PREF
+#define LMM_TPS_PREF LMM_TPP_PREF
+#endif
+#ifndef LMM_TPS_PREF_PHILOX
+#define LMM_TPS_PREF_PHILOX 1
+#endif
 
 template <int NN, int NMAT>
 struct TpsLayout {
@@ -965,7 +993,8 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
 {
     using Lay = TpsLayout<NN, NMAT>;
     constexpr int B = Lay::B, H = Lay::H, M = Lay::M, NOUT = Lay::NOUT, PAD = NMAT;
-    constexpr int G = LMM_TPP_SKEW, RCH = PHILOX ? LMM_TPP_RCHUNK_PHILOX : LMM_TPP_RCHUNK;
+    constexpr int G = LMM_TPP_SKEW, RCH = PHILOX ? LMM_TPS_RCHUNK_PHILOX : LMM_TPS_RCHUNK;
+    constexpr int PF = PHILOX ? LMM_TPS_PREF_PHILOX : LMM_TPS_PREF;
     static_assert(NMAT % 4 == 0 && NMAT % G == 0, "normals in quads, reverse steps in groups");
     static_assert(RCH - 1 <= Lay::VPAD, "the windows' spare vega rows lie inside the table");
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1023,7 +1052,7 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                 for (int i = 0; i < NN; ++i) IL[i] = il0_s[i];
                 float4 zq, zq_next = zquad<PHILOX, NMAT>(zp, seed, gpath, 0);
                 for (int n = 0; n < NMAT; n += 2) {
-                    if (LMM_TPS_SYNC && (n % (2 * (PHILOX ? LMM_TPP_FSYNC_PHILOX : LMM_TPP_FSYNC))) == 0)
+                    if (LMM_TPS_SYNC && (n % (2 * (PHILOX ? LMM_TPS_FSYNC_PHILOX : LMM_TPS_FSYNC))) == 0)
                         __syncthreads();
                     if ((n & 3) == 0) {
                         zq = zq_next;
@@ -1032,7 +1061,7 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                     const float sqez0 = sqd * ((n & 2) ? zq.z : zq.x);
                     const float sqez1 = sqd * ((n & 2) ? zq.w : zq.y);
                     float V0, V1, V0c, V1c;
-                    fwd_pair_window_cap<NN, LMM_TPP_CHUNK, kPref<PHILOX>, H - 1>(IL, kc0 - (n + 1), sqez0, sqez1,
+                    fwd_pair_window_cap<NN, LMM_TPP_CHUNK, PF, H - 1>(IL, kc0 - (n + 1), sqez0, sqez1,
                                                                                 delta, n, V0, V1, V0c, V1c);
                     vt0[n * B] = V0;
                     vt0[(n + 1) * B] = V1;
@@ -1068,7 +1097,7 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                     st[g].kc = kc0 - (mm + 1) + H;
                     st[g].vg = vg0 + (H - mm - 1) * B;
                 }
-                rev_half_window<H, H, B, G, RCH, kPref<PHILOX>>(Xu, Pu, st, delta, n);
+                rev_half_window<H, H, B, G, RCH, PF>(Xu, Pu, st, delta, n);
 #pragma unroll
                 for (int g = 0; g < G; ++g) sc[(Lay::s_s + n - g) * B] = st[g].S;
             }
@@ -1107,7 +1136,7 @@ k_tps(const DevModel m, const float *__restrict__ z, uint64_t seed, int64_t path
                         ns[g] = sc[(Lay::s_s + n - G - g) * B];
                     }
                 }
-                rev_half_window<H, 0, B, G, RCH, kPref<PHILOX>>(Xl, Pl, st, delta, n);
+                rev_half_window<H, 0, B, G, RCH, PF>(Xl, Pl, st, delta, n);
             }
 
             // ---- cross-path reduction of this batch of B paths ----
