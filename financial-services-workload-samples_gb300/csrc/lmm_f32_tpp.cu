@@ -1212,10 +1212,14 @@ cudaError_t occ_tps(int *blocks)
 // k_tpq: the fused long-tenor call (NN = 160, NMAT = 120) with one thread per
 // path, the reverse sweep in passes over blocks of 40 rates.
 //
-// The forward holds all NN inverse rates in registers (about 200 registers:
-// 8 warps, 256 paths per SM) and saves, per step, the drift sum at the top
-// rate of every block and the rates every ck steps (ck = DevModel::ckpt, a
-// multiple of 4). The reverse then runs the blocks one after another from the
+// The forward runs in two passes of 80 rates through one copy of the pass
+// body (rates 0..79 for the steps that move them, then rates 80..159 for
+// every step from the first pass's drift sums at rate 79), so at most 80
+// inverse rates are live (255 registers in all: 8 warps, 256 paths per SM,
+// the vega rows of 256 paths fill shared memory), and saves, per step, the
+// drift sum at the top rate of every block and the rates every ck steps
+// (ck = DevModel::ckpt, a multiple of 4); the per-maturity constants are read
+// from shared memory. The reverse then runs the blocks one after another from the
 // top, in one thread: block b (rates 40b .. 40b+39) for every group of four
 // steps with an active cell in it, each step starting from the forward's
 // drift sum at the block's top rate and from the suffix sum the block above
