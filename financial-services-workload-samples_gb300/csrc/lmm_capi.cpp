@@ -902,18 +902,21 @@ int lmm_swaption_breakdown_f64_device(lmm_engine *e, const double *d_z, int64_t 
 // pieces on the engine's copy stream; the fused kernel of piece c starts as
 // soon as piece c has landed, while the later pieces are still in flight.
 // Relative piece sizes kHostSplit: the first piece's copy is the only one
-// nothing overlaps, so it is small (1/36: 3 waves, 19 MB of 671 MB at 4M
-// paths, 0.09 ms at the measured 211 GB/s), and each later piece lands
-// before the compute of the pieces ahead of it ends (at 4M paths: 9, 24 and
-// 72 waves). Measured on GB300 at 4,194,304 paths: four equal pieces cost 0.6
-// ms per call more than {1,3,6,6}/16 (an earlier kernel); piece boundaries on
-// whole device waves: 363 -> 369 M paths/s; {1,3,10,22}/36: 369 -> 373 M
-// paths/s; with the 9.8 ms kernel, {1,3,10,22}, {1,2,5,10,18}, {1,2,4,8,21},
-// {1,3,8,24}, {1,4,31}: 10.07, 10.05, 10.06, 10.03, 11.70 ms per call. Each
-// piece writes its own range of partial sums and one ordered k_finalize
+// nothing overlaps, so it is small (1/72: one wave of the split-reverse
+// kernel, 9 MB of 671 MB at 4M paths, 0.04 ms at the measured 211 GB/s), and
+// each later piece, about three times the one before, lands before the
+// compute of the pieces ahead of it ends (a wave computes in about 0.14 ms
+// and copies in 0.04 ms). Measured on GB300 at 4,194,304 paths: four equal
+// pieces cost 0.6 ms per call more than {1,3,6,6}/16 (an earlier kernel);
+// piece boundaries on whole device waves: 363 -> 369 M paths/s;
+// {1,3,10,22}/36: 369 -> 373 M paths/s; with the 9.8 ms kernel,
+// {1,3,10,22}, {1,2,5,10,18}, {1,2,4,8,21}, {1,3,8,24}, {1,4,31}: 10.07,
+// 10.05, 10.06, 10.03, 11.70 ms per call, and {1,3,8,24}, {1,3,9,27,32},
+// {1,2,6,18,45}, {1,4,16,51}, {1,3,9,59}: 10.04, 10.02, 10.02, 10.23, 11.32.
+// Each piece writes its own range of partial sums and one ordered k_finalize
 // covers them all. Single-scenario engines only.
 #ifndef LMM_HOST_SPLIT
-#define LMM_HOST_SPLIT 1, 3, 8, 24
+#define LMM_HOST_SPLIT 1, 2, 6, 18, 45
 #endif
 constexpr int kHostSplit[] = {LMM_HOST_SPLIT};
 constexpr int kHostChunks = sizeof(kHostSplit) / sizeof(kHostSplit[0]);

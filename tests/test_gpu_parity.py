@@ -347,10 +347,11 @@ def test_fp32_range_is_never_silently_wrong(P):
     np.testing.assert_allclose(g64[0], m, rtol=1e-9, atol=1e-10 * np.abs(m).max())
 
 
-def _host_pieces(paths, sms, blocks_per_sm=1, per_block=256, split=(1, 3, 10, 22)):
+def _host_pieces(paths, sms, blocks_per_sm=1, per_block=384, split=(1, 2, 6, 18, 45)):
     """The pieces the pipelined host call cuts `paths` into: boundaries at the
-    cumulative shares of `split`, rounded to whole waves of the device
-    (sms x blocks per SM x paths per block), empty pieces dropped."""
+    cumulative shares of `split` (LMM_HOST_SPLIT), rounded to whole waves of
+    the device (sms x blocks per SM x paths per block: one 384-path block per
+    SM for the fused 80/40 kernel), empty pieces dropped."""
     wave = sms * blocks_per_sm * per_block
     tot, cum, bnd = sum(split), 0, [0]
     for c in range(1, len(split)):
