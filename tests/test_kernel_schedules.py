@@ -293,7 +293,7 @@ def half_window(n, G, ch, p, H, lo, nn=TPP_NN):
     return flushes, {lo + j - n - 1 for j in consts}
 
 
-@pytest.mark.parametrize("ch", [2, 4])
+@pytest.mark.parametrize("ch", [1, 2, 4])
 def test_split_reverse_half_windows(ch):
     """k_tps: the upper half (rates 40..79) and then the lower half (rates
     0..39) over every group of four steps flush every active cell's vega
