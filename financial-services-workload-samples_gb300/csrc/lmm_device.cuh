@@ -46,7 +46,7 @@ __device__ __forceinline__ float ex2_approx(float x)
 
 // Two reciprocals from one: 1/a = b/(ab), 1/b = a/(ab). The forward's a, b
 // are 1/L + delta >= delta; ab overflows FP32 only if both rates fall below
-// about 5e-20 (from L0 >= 1e-3, some 40 standard deviations of the
+// about 5e-20 (from L0 >= 1e-3, more than 30 standard deviations of the
 // log-rate's spread over 40 steps at lambda = 0.35), so the product stays
 // far inside the range.
 __device__ __forceinline__ void rcp_pair(float a, float b, float &ta, float &tb)
